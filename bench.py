@@ -1,0 +1,406 @@
+"""Culling benchmark: culled object-views/s of the batched persistent CUDA path (bit-exact),
+next to the plain per-call path, the roofline of the cull kernel, end-to-end throughput
+through the C ABI with host buffers, and the reference CPU path on the host cores.
+
+Default workload (the bandwidth stress configuration): 16M objects over 1M shared world
+matrices, 8 simultaneous views (6 cube faces + a stereo pair), seeded synthetic data.  A
+step is one batched cull of all objects in all views under a new camera (jittered by up
+to 2 degrees per step, so the changed lists are not empty).
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+                    [--workload stress|plain|hierarchy|batched]
+
+N > 1 runs under torch.distributed.run, one process per GPU: every rank culls its own
+shard (its own 16M objects) -- weak scaling, no data-path collective; the barrier and
+the max over ranks of the timed region use torch.distributed.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import shutil
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+from pipeline_gb300 import workloads as W  # noqa: E402
+
+STRESS_N, STRESS_T = 16_000_000, 1_000_000
+
+
+def peaks() -> dict:
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        d = json.loads(p.read_text())
+        return {"hbm_gbs": float(d["hbm_gbs"]), "source": "measured"}
+    return {"hbm_gbs": 6800.0, "source": "fallback"}
+
+
+# ---- distributed plumbing ----------------------------------------------------------------
+class Dist:
+    def __init__(self, want: int):
+        self.world = int(os.environ.get("WORLD_SIZE", "1"))
+        self.rank = int(os.environ.get("RANK", "0"))
+        self.local = int(os.environ.get("LOCAL_RANK", "0"))
+        self.pg = None
+        if self.world > 1:
+            import torch
+            import torch.distributed as dist
+
+            torch.cuda.set_device(self.local)
+            dist.init_process_group("nccl")
+            self.pg = dist
+
+    def barrier(self):
+        if self.pg:
+            self.pg.barrier()
+
+    def max(self, x: float) -> float:
+        if not self.pg:
+            return x
+        import torch
+
+        t = torch.tensor([x], dtype=torch.float64, device=f"cuda:{self.local}")
+        self.pg.all_reduce(t, op=self.pg.ReduceOp.MAX)
+        return float(t.item())
+
+    def close(self):
+        if self.pg:
+            self.pg.destroy_process_group()
+
+
+# ---- clocks --------------------------------------------------------------------------------
+class Clocks:
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device: int):
+        self.device = device
+        self.proc = None
+        self.path = None
+
+    def start(self):
+        exe = shutil.which("nvidia-smi")
+        if not exe:
+            return
+        fd, self.path = tempfile.mkstemp(suffix=".csv")
+        os.close(fd)
+        self.proc = subprocess.Popen([exe, f"--id={self.device}", f"--query-gpu={self.FIELDS}",
+                                      "--format=csv,noheader,nounits", "-lms", "200"],
+                                     stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        time.sleep(0.3)
+
+    def stop(self) -> dict | None:
+        if not self.proc:
+            return None
+        time.sleep(0.25)
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        rows = []
+        for line in Path(self.path).read_text().splitlines():
+            parts = [x.strip() for x in line.split(",")]
+            if len(parts) >= 9:
+                rows.append(parts)
+        os.unlink(self.path)
+        if not rows:
+            return None
+        sm = [float(r[1]) for r in rows if r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in rows if r[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for r in rows for i in range(4) if r[5 + i].lower().startswith("active")})
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(rows)}
+
+
+# ---- workloads -------------------------------------------------------------------------------
+def make_frames(rng, base_vps, steps):
+    """One view set per step: the base views, each rotated by up to 2 degrees."""
+    return [np.stack([W.jitter_view(rng, v) for v in base_vps]) for _ in range(steps)]
+
+
+class Stress:
+    name = "stress"
+
+    def __init__(self, seed: int, n: int = STRESS_N, t: int = STRESS_T):
+        self.sc = W.stress_scene(seed=seed, n_objects=n, n_transforms=t)
+        self.n, self.t, self.v = n, t, self.sc["vps"].shape[0]
+        self.describe = (f"bandwidth stress: {n // 1_000_000}M objects over {t // 1_000_000}M shared world "
+                         f"matrices (index uniform), {self.v} views (6 cube faces + stereo pair, 6.5 cm), "
+                         "FP32 SoA, new camera per step (jitter <= 2 deg)")
+
+    def setup(self, ctx, tuning=None):
+        from pipeline_gb300 import native  # noqa: F401
+
+        sc = self.sc
+        self.g = ctx.group_create()
+        ctx.group_set_objects(self.g, sc["lower"], sc["extent"], sc["xform"])
+        ctx.group_set_matrices(self.g, sc["mats"])
+        self.rs = [ctx.result_create(self.g) for _ in range(self.v)]
+        self.rp = [ctx.result_create(self.g) for _ in range(self.v)]
+        self.plan = ctx.plan_create([(self.g, self.rs, sc["vps"])], tuning)
+        self.referenced = int(np.unique(sc["xform"]).size)
+
+    def object_views(self) -> int:
+        return self.n * self.v
+
+    def algorithmic_bytes(self, changed_total: int) -> int:
+        words = (self.n + 31) // 32
+        return (28 * self.n + 64 * self.referenced + 64 * self.v + self.v * words * 4 * 2
+                + 4 * changed_total)
+
+
+# ---- our arm ---------------------------------------------------------------------------------
+def run_ours(args, dist: Dist) -> dict | None:
+    import torch
+
+    from pipeline_gb300 import build, native
+
+    if dist.rank == 0 or not (ROOT / "pipeline_gb300" / "_lib" / "libdpcull.so").exists():
+        build.build_all()
+    dist.barrier()
+    device = dist.local
+    torch.cuda.set_device(device)
+    wl = Stress(seed=3 + 1000 * dist.rank)
+    ctx = native.Context(device)
+    wl.setup(ctx, json.loads(args.tuning) if args.tuning else None)
+    tuning = ctx.plan_tuning(wl.plan)
+    rng = np.random.default_rng(17 + dist.rank)
+    frames = make_frames(rng, wl.sc["vps"], args.warmup + args.steps + 1)
+    stream = torch.cuda.ExternalStream(ctx.stream)
+
+    # -- batched persistent path (graph replay), device-resident inputs --
+    for i in range(args.warmup):
+        ctx.plan_set_views(wl.plan, frames[i])
+        ctx.plan_launch(wl.plan)
+    ctx.synchronize()
+    ev = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps + 1)]
+    clocks = Clocks(device)
+    clocks.start()
+    dist.barrier()
+    torch.cuda.synchronize()
+    launches0 = ctx.kernel_launches
+    with torch.cuda.stream(stream):
+        ev[0].record(stream)
+        for i in range(args.steps):
+            ctx.plan_set_views(wl.plan, frames[args.warmup + i])
+            ctx.plan_launch(wl.plan)
+            ev[i + 1].record(stream)
+    ctx.synchronize()
+    torch.cuda.synchronize()
+    launches = ctx.kernel_launches - launches0
+    clk = clocks.stop()
+    step_ms = [ev[i].elapsed_time(ev[i + 1]) for i in range(args.steps)]
+    total_ms = ev[0].elapsed_time(ev[args.steps])
+    total_ms = dist.max(total_ms)
+    dist.barrier()
+    changed = [len(ctx.result_changed(r)) for r in wl.rs]
+    ms_step = total_ms / args.steps
+    value = wl.object_views() * dist.world / (ms_step / 1e3)
+
+    # -- plain per-call path: one launch per view and cull call --
+    for i in range(2):
+        for v in range(wl.v):
+            ctx.cull(wl.g, wl.rp[v], frames[i][v])
+    ctx.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    plain_steps = max(3, min(args.steps, 20))
+    with torch.cuda.stream(stream):
+        e0.record(stream)
+        for i in range(plain_steps):
+            for v in range(wl.v):
+                ctx.cull(wl.g, wl.rp[v], frames[args.warmup + i][v])
+        e1.record(stream)
+    ctx.synchronize()
+    plain_ms = dist.max(e0.elapsed_time(e1) / plain_steps)
+
+    # -- parity spot check after the timed region: every view, first 256k objects --
+    parity = parity_sample(ctx, wl, frames[args.warmup + args.steps - 1])
+
+    # -- end to end through the C ABI with host buffers --
+    e2e = run_e2e(ctx, wl, frames, args, dist)
+
+    bytes_launch = wl.algorithmic_bytes(sum(changed))
+    pk = peaks()
+    achieved = bytes_launch / (ms_step / 1e3) / 1e9
+    traffic = traffic_from_profile(wl)
+    out = {
+        "metric": "culled object-views/s (batched persistent launch, bit-exact vs reference CPU manager)",
+        "value": value, "unit": "object-views/s", "n_gpus": dist.world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded; the reference publishes no dataset)",
+        "config": {"workload": wl.describe, "objects_per_gpu": wl.n, "transforms": wl.t, "views": wl.v,
+                   "parallelism": f"{dist.world} independent object shards (no collective)",
+                   "l2": "no flush: per-step object data (448 MB) exceeds L2 (126 MB)",
+                   "tuning": tuning},
+        "latency_ms": {"p50": float(np.percentile(step_ms, 50)), "p99": float(np.percentile(step_ms, 99)),
+                       "max": float(max(step_ms))},
+        "plain": {"value": wl.object_views() * dist.world / (plain_ms / 1e3), "ms_per_step": plain_ms,
+                  "launches_per_step": wl.v},
+        "batched_vs_plain": plain_ms / ms_step,
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": pk["hbm_gbs"], "unit": "GB/s",
+                     "frac": achieved / pk["hbm_gbs"], "traffic": traffic,
+                     "peak_source": pk["source"], "algorithmic_bytes_per_launch": bytes_launch,
+                     "kernel": "cull_kernel (persistent, graph replay; event time per step)"},
+        "e2e": e2e, "gpu_launches": launches, "clocks": clk, "parity_sample": parity,
+        "changed_per_step": changed,
+    }
+    ctx.close()
+    return out
+
+
+def parity_sample(ctx, wl, vps, m: int = 262_144) -> dict:
+    import oracle
+
+    sc = wl.sc
+    obbs = oracle.build_obbs(sc["lower"][:, :m], sc["extent"][:, :m], sc["xform"][:m], sc["mats"])
+    ok = True
+    for v, r in enumerate(wl.rs):
+        gpu = ctx.result_bits(r)[: m // 32]
+        ok &= bool(np.array_equal(gpu, oracle.cull_obbs(obbs, vps[v], threads=8)))
+    return {"objects": m, "views": len(wl.rs), "bit_exact": ok}
+
+
+def run_e2e(ctx, wl, frames, args, dist) -> dict:
+    """Steps through the public API with host buffers: H2D of the step's view matrices from
+    pinned memory, the batched cull, D2H of every view's visibility words and changed list."""
+    import torch
+
+    words = (wl.n + 31) // 32
+    bits = [torch.empty(words, dtype=torch.int32, pin_memory=True).numpy().view(np.uint32)
+            for _ in range(wl.v)]
+    changed = [torch.empty(wl.n, dtype=torch.int32, pin_memory=True).numpy().view(np.uint32)
+               for _ in range(wl.v)]
+    vps_pinned = torch.empty((wl.v, 16), dtype=torch.float32, pin_memory=True).numpy()
+    steps = max(3, min(args.steps, 20))
+    d2h = 0
+    dist.barrier()
+    t0 = time.perf_counter()
+    for i in range(steps):
+        vps_pinned[:] = frames[i % len(frames)]
+        ctx.plan_set_views(wl.plan, vps_pinned)
+        ctx.plan_launch(wl.plan)
+        for v in range(wl.v):
+            ctx.result_bits(wl.rs[v], bits[v])
+            ch = ctx.result_changed(wl.rs[v], changed[v])
+            d2h += words * 4 + 4 + 4 * len(ch)
+    dt = dist.max(time.perf_counter() - t0)
+    return {"value": wl.object_views() * dist.world * steps / dt, "unit": "object-views/s",
+            "ms_per_step": dt * 1e3 / steps, "h2d_bytes_per_step": wl.v * 64,
+            "d2h_bytes_per_step": int(d2h / steps), "steps": steps,
+            "path": "plan_set_views + plan_launch + result_bits + result_changed (C ABI)"}
+
+
+def traffic_from_profile(wl) -> int | None:
+    """DRAM bytes per launch from the committed ncu summary, scaled to this workload."""
+    p = ROOT / "profiles" / "cull_stress_traffic.json"
+    if not p.exists():
+        return None
+    d = json.loads(p.read_text())
+    scale = (wl.n * wl.v) / (d["objects"] * d["views"])
+    return int(d["dram_bytes_per_launch"] * scale)
+
+
+# ---- CPU baseline (oracle port on the host cores) ----------------------------------------------
+def cpu_baseline(wl, sample: int, threads: int, reps: int = 3) -> dict:
+    import oracle
+
+    sc = wl.sc
+    m = min(sample, wl.n)
+    obbs = oracle.build_obbs(sc["lower"][:, :m], sc["extent"][:, :m], sc["xform"][:m], sc["mats"])
+    prev = [np.zeros((m + 31) // 32, np.uint32) for _ in range(wl.v)]
+    ts = []
+    for _ in range(reps):
+        t0 = time.perf_counter()
+        for v in range(wl.v):
+            bits = oracle.cull_obbs(obbs, sc["vps"][v], threads=threads)
+            oracle.update_changed(prev[v], bits, m)
+        ts.append(time.perf_counter() - t0)
+    t_warm = statistics.median(ts)
+    t0 = time.perf_counter()
+    oracle.build_obbs(sc["lower"][:, :m], sc["extent"][:, :m], sc["xform"][:m], sc["mats"])
+    t_obb = time.perf_counter() - t0
+    return {"value": m * wl.v / t_warm, "unit": "object-views/s", "cores": threads, "kind": "port",
+            "sample": f"first {m} objects x {wl.v} views, OBB cache warm, median of {reps}",
+            "cold_value": m * wl.v / (t_warm + t_obb)}
+
+
+def run_reference(args, dist: Dist) -> dict | None:
+    """The reference CPU culling path (oracle port of cpu::ManagerImpl::cull +
+    ResultBitSet::updateChanged) on all host cores, same workload and metric."""
+    if dist.rank != 0:
+        return None
+    import oracle
+
+    oracle.build(with_reference=False)
+    threads = os.cpu_count() or 1
+    wl = Stress(seed=3)
+    sample = 2_000_000
+    m = sample
+    sc = wl.sc
+    obbs = oracle.build_obbs(sc["lower"][:, :m], sc["extent"][:, :m], sc["xform"][:m], sc["mats"])
+    prev = [np.zeros((m + 31) // 32, np.uint32) for _ in range(wl.v)]
+    rng = np.random.default_rng(17)
+    frames = make_frames(rng, sc["vps"], args.warmup + args.steps)
+    ts = []
+    for i in range(args.warmup + args.steps):
+        t0 = time.perf_counter()
+        for v in range(wl.v):
+            bits = oracle.cull_obbs(obbs, frames[i][v], threads=threads)
+            oracle.update_changed(prev[v], bits, m)
+        if i >= args.warmup:
+            ts.append(time.perf_counter() - t0)
+    t = sum(ts) / len(ts)
+    value = m * wl.v / t
+    desc = f"first {m} objects of the workload x {wl.v} views per step (warm OBB cache), {threads} threads"
+    return {"impl": "reference", "metric": "culled object-views/s (batched persistent launch, bit-exact vs reference CPU manager)",
+            "value": value, "unit": "object-views/s", "n_gpus": dist.world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": t * 1e3, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": {"workload": wl.describe, "objects_per_gpu": wl.n, "views": wl.v},
+            "cpu_baseline": {"value": value, "unit": "object-views/s", "cores": threads, "kind": "port",
+                             "sample": desc},
+            "e2e": {"value": value, "unit": "object-views/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=50)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--workload", default="stress", choices=["stress"])
+    ap.add_argument("--tuning", default=None, help="JSON tuning (default: autotuner)")
+    ap.add_argument("--cpu-sample", type=int, default=1_000_000)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    args.warmup = max(args.warmup, 3)
+    dist = Dist(args.gpus)
+    if args.impl == "reference":
+        out = run_reference(args, dist)
+    else:
+        out = run_ours(args, dist)
+        if out is not None and dist.rank == 0 and not args.no_cpu_baseline:
+            wl_cpu = Stress(seed=3, n=min(args.cpu_sample, STRESS_N))
+            out["cpu_baseline"] = cpu_baseline(wl_cpu, args.cpu_sample, 1)
+            out["cpu_baseline"]["all_cores"] = cpu_baseline(wl_cpu, args.cpu_sample, os.cpu_count() or 1, reps=3)
+    if out is not None and dist.rank == 0:
+        print(json.dumps(out))
+    dist.close()
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,200 @@
+/*
+ * dpcull.h -- C ABI of the GB300 culling backend for nvpro-pipeline.
+ *
+ * This is the boundary a dp::culling::cuda::Manager (the Mode::CUDA backend that the
+ * reference declares in dp/culling/Manager.h:98 but never implements) and a
+ * dp::transform tree binding reach the GPU through.  Plain C types only: pointers,
+ * sizes and integer handles; no exceptions cross it.  Every function returns
+ * DPCULL_OK (0) or a negative DPCULL_ERR_* code; dpcull_last_error() gives the
+ * message of the calling thread's last failure.
+ *
+ * Conventions (the reference's, dp/math/Matmnt.h): a matrix is 16 floats, row-major,
+ * row-vector convention (v' = v * M, world = local * parentWorld, clip = p * VP).
+ * Visibility bit i of 32-bit word i/32 is object i of the group (ResultBitSet layout).
+ * Object data is passed in planar form: lower[3][n] is the x row, then the y row, then
+ * the z row of the boxes' lower corners; extent[3][n] likewise holds upper - lower,
+ * exactly as ManagerBitSet::objectSetBoundingBox stores them
+ * (dp/culling/src/ManagerBitSet.cpp:99-109).
+ *
+ * Results are bit-exact with the reference CPU manager (cpu::ManagerImpl::cull,
+ * dp/culling/cpu/src/ManagerImpl.cpp:467-518) and transform tree
+ * (dp/transform/src/Tree.cpp:133-166).
+ *
+ * Threading: a context owns one CUDA stream; calls on one context must not overlap.
+ * Calls marked (async) only enqueue work; calls that return data to host memory
+ * synchronize the context's stream first.
+ */
+#ifndef DPCULL_H
+#define DPCULL_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define DPCULL_OK 0
+#define DPCULL_ERR_INVALID_ARGUMENT (-1) /* bad handle, null pointer, bad size */
+#define DPCULL_ERR_OUT_OF_RANGE (-2)     /* transform index >= matrix count, bad object index */
+#define DPCULL_ERR_CUDA (-3)             /* a CUDA runtime call failed */
+#define DPCULL_ERR_NO_MEMORY (-4)        /* device or pinned allocation failed */
+#define DPCULL_ERR_STATE (-5)            /* call not valid in the current state */
+#define DPCULL_ERR_TIMEOUT (-6)          /* a bounded device-side wait expired */
+#define DPCULL_ERR_CAPACITY (-7)         /* caller's output buffer is too small */
+
+typedef struct dpcull_ctx_s* dpcull_ctx;
+typedef uint32_t dpcull_group;
+typedef uint32_t dpcull_result;
+typedef uint32_t dpcull_tree;
+typedef uint32_t dpcull_plan;
+
+/* Last error message of the calling thread ("" if none). */
+const char* dpcull_last_error(void);
+/* Library version, (major << 16) | minor. */
+uint32_t dpcull_version(void);
+
+/* ---- context ----------------------------------------------------------------------
+ * Replaces the reference's Manager factory (cpu::Manager::create,
+ * dp/culling/cpu/Manager.h:39-43).  device: CUDA ordinal; stream: a cudaStream_t to
+ * work on, or NULL to let the context create its own. */
+int dpcull_ctx_create(int device, void* stream, dpcull_ctx* out);
+int dpcull_ctx_destroy(dpcull_ctx ctx);
+/* Waits for all enqueued work; reports device-side errors (bad transform index,
+ * expired wait) raised since the last check. */
+int dpcull_ctx_synchronize(dpcull_ctx ctx);
+/* The context's cudaStream_t. */
+void* dpcull_ctx_stream(dpcull_ctx ctx);
+/* Number of kernels this context has launched (graph launches count their kernels). */
+uint64_t dpcull_ctx_kernel_launches(dpcull_ctx ctx);
+/* Device bytes currently held by the context. */
+uint64_t dpcull_ctx_device_bytes(dpcull_ctx ctx);
+
+/* ---- groups: a GroupBitSet's objects and matrices resident in HBM -------------------
+ * Replaces Manager::groupCreate (dp/culling/Manager.h:119). */
+int dpcull_group_create(dpcull_ctx ctx, dpcull_group* out);
+int dpcull_group_destroy(dpcull_ctx ctx, dpcull_group g);
+/* Replaces the group's objects with n new ones (groupAddObject x n after
+ * objectSetBoundingBox / objectSetTransformIndex, Manager.h:113-120).  Host arrays. */
+int dpcull_group_set_objects(dpcull_ctx ctx, dpcull_group g, size_t n, const float* lower,
+                             const float* extent, const uint32_t* xform);
+/* Appends k objects at indices n..n+k-1 (GroupBitSet::addObject,
+ * dp/culling/src/GroupBitSet.cpp:76-91). */
+int dpcull_group_append_objects(dpcull_ctx ctx, dpcull_group g, size_t k, const float* lower,
+                                const float* extent, const uint32_t* xform);
+/* Overwrites the listed objects in place (objectSetBoundingBox /
+ * objectSetTransformIndex on grouped objects, ManagerBitSet.cpp:88-109). */
+int dpcull_group_update_objects(dpcull_ctx ctx, dpcull_group g, size_t k, const uint32_t* index,
+                                const float* lower, const float* extent, const uint32_t* xform);
+/* Removes object `index` by moving the last object into its slot and remapping every
+ * result's bit (GroupBitSet::removeObject + ResultBitSet::onNotify,
+ * GroupBitSet.cpp:93-119, ResultBitSet.cpp:110-128). */
+int dpcull_group_remove_object(dpcull_ctx ctx, dpcull_group g, size_t index);
+int dpcull_group_count(dpcull_ctx ctx, dpcull_group g, size_t* n);
+/* Copies `count` matrices from host memory at `matrices` with a byte stride into the
+ * group's device matrix array (groupSetMatrices, Manager.h:124; the data is read now,
+ * as the reference reads it when its cached boxes are rebuilt). */
+int dpcull_group_set_matrices(dpcull_ctx ctx, dpcull_group g, const void* matrices, size_t count,
+                              size_t stride);
+/* Re-uploads only the listed matrices, read from matrices + index*stride
+ * (groupMatrixChanged, Manager.h:125, as a dirty scatter). */
+int dpcull_group_update_matrices(dpcull_ctx ctx, dpcull_group g, size_t k, const uint32_t* index,
+                                 const void* matrices, size_t stride);
+/* Uses a device matrix array in place (16-byte aligned, count x 16 floats), e.g. the
+ * world matrices of a dpcull tree; no copy.  The caller keeps it alive. */
+int dpcull_group_bind_device_matrices(dpcull_ctx ctx, dpcull_group g, const float* dev_matrices,
+                                      size_t count);
+/* Manager::getBoundingBox (Manager.h:142, ManagerBitSet.cpp:151-306), bit-exact. */
+int dpcull_group_bounding_box(dpcull_ctx ctx, dpcull_group g, float lower[3], float upper[3]);
+
+/* ---- results ------------------------------------------------------------------------
+ * Replaces Manager::groupCreateResult (Manager.h:126).  A result starts with every
+ * object visible, as ResultBitSet does on first use (ResultBitSet.cpp:65-79). */
+int dpcull_result_create(dpcull_ctx ctx, dpcull_group g, dpcull_result* out);
+int dpcull_result_destroy(dpcull_ctx ctx, dpcull_result r);
+/* (async) Manager::cull (Manager.h:139): visibility of every object of g under vp
+ * (16 floats, host memory), stored in r together with the ascending list of objects whose
+ * visibility changed since r's previous cull. */
+int dpcull_cull(dpcull_ctx ctx, dpcull_group g, dpcull_result r, const float vp[16]);
+/* Manager::resultGetChanged (Manager.h:129): copies the changed list (group indices,
+ * ascending) to host memory; *n receives its length.  DPCULL_ERR_CAPACITY if cap < *n. */
+int dpcull_result_changed(dpcull_ctx ctx, dpcull_result r, uint32_t* out, size_t cap, size_t* n);
+/* Visibility words of r (ceil(n/32) words); *n_bits receives the object count. */
+int dpcull_result_bits(dpcull_ctx ctx, dpcull_result r, uint32_t* out, size_t n_words,
+                       size_t* n_bits);
+/* Manager::resultObjectIsVisible (Manager.h:132) for group index `index`. */
+int dpcull_result_is_visible(dpcull_ctx ctx, dpcull_result r, size_t index, int* visible);
+/* Device pointers of r's visibility words, changed list and changed count. */
+int dpcull_result_device(dpcull_ctx ctx, dpcull_result r, uint32_t** bits, uint32_t** changed,
+                         uint32_t** n_changed);
+
+/* ---- batched multi-scene, multi-view culling ----------------------------------------
+ * One job culls one group under n_views view-projections into n_views results (one
+ * result per view, each bound to that group).  All jobs run in one persistent launch. */
+typedef struct dpcull_job {
+  dpcull_group group;
+  uint32_t n_views;
+  const dpcull_result* results; /* n_views results of `group` */
+  const float* vps;             /* n_views x 16 floats, host memory */
+} dpcull_job;
+
+typedef struct dpcull_tuning {
+  uint32_t views_per_pass;   /* 1, 2, 4 or 8 views evaluated per object load ("views per warp") */
+  uint32_t tiles_per_ticket; /* tiles a CTA claims at once ("tiles per CTA") */
+  uint32_t ctas_per_sm;      /* persistent CTAs per SM (0 = occupancy limit) */
+  uint32_t reserved;
+} dpcull_tuning;
+
+/* (async) One persistent launch over all jobs.  tuning may be NULL (defaults). */
+int dpcull_cull_batched(dpcull_ctx ctx, const dpcull_job* jobs, size_t n_jobs,
+                        const dpcull_tuning* tuning);
+/* Builds a reusable plan for a fixed job list and captures its launch (view upload
+ * included) in a CUDA graph.  tuning NULL = run the autotuner (cached per shape). */
+int dpcull_plan_create(dpcull_ctx ctx, const dpcull_job* jobs, size_t n_jobs,
+                       const dpcull_tuning* tuning, dpcull_plan* out);
+/* Replaces the plan's view-projections (sum of n_views x 16 floats, job order). */
+int dpcull_plan_set_views(dpcull_ctx ctx, dpcull_plan p, const float* vps);
+/* (async) Replays the plan's graph. */
+int dpcull_plan_launch(dpcull_ctx ctx, dpcull_plan p);
+int dpcull_plan_tuning(dpcull_ctx ctx, dpcull_plan p, dpcull_tuning* out);
+int dpcull_plan_destroy(dpcull_ctx ctx, dpcull_plan p);
+/* Autotunes views_per_pass / tiles_per_ticket / ctas_per_sm for the job list by timing
+ * candidate launches (results of the jobs are overwritten). */
+int dpcull_autotune(dpcull_ctx ctx, const dpcull_job* jobs, size_t n_jobs, dpcull_tuning* out);
+
+/* ---- transform tree (dp::transform::Tree, dp/transform/Tree.h:42-129) ----------------
+ * The host keeps the tree's structure (levels of (parent, transform) entries in the
+ * reference's list order); the device keeps local and world matrices. */
+int dpcull_tree_create(dpcull_ctx ctx, size_t capacity, dpcull_tree* out);
+int dpcull_tree_destroy(dpcull_ctx ctx, dpcull_tree t);
+/* Grows the capacity keeping every matrix and dirty bit (Tree::resizeDataStructures,
+ * Tree.cpp:117-126; new entries are zero). */
+int dpcull_tree_resize(dpcull_ctx ctx, dpcull_tree t, size_t capacity);
+/* Level lists: pairs[2*i] = parent, pairs[2*i+1] = transform, level l spanning
+ * [level_offsets[l], level_offsets[l+1]).  Replaces the structure set by addTransform /
+ * removeTransform (Tree.cpp:54-98). */
+int dpcull_tree_set_structure(dpcull_ctx ctx, dpcull_tree t, size_t n_entries,
+                              const uint32_t* pairs, size_t n_levels,
+                              const uint32_t* level_offsets);
+/* Tree::updateLocalMatrix (Tree.h:87) for k transforms: writes the locals and marks
+ * them dirty.  Matrices in host memory, 16 floats each. */
+int dpcull_tree_set_locals(dpcull_ctx ctx, dpcull_tree t, size_t k, const uint32_t* index,
+                           const float* matrices);
+/* Sets world[index] without marking anything dirty (the fixed root, Tree.cpp:38-47). */
+int dpcull_tree_set_worlds(dpcull_ctx ctx, dpcull_tree t, size_t k, const uint32_t* index,
+                           const float* matrices);
+/* (async) Tree::compute (Tree.cpp:133-166): propagates world matrices level by level;
+ * afterwards the dirty-world bits of this pass are readable and the dirty-local bits
+ * are clear. */
+int dpcull_tree_compute(dpcull_ctx ctx, dpcull_tree t);
+/* Device pointer and capacity of the world matrix array (Tree::getWorldMatrices). */
+int dpcull_tree_world_device(dpcull_ctx ctx, dpcull_tree t, const float** world, size_t* count);
+/* Copies world matrices [first, first+count) to host memory. */
+int dpcull_tree_world(dpcull_ctx ctx, dpcull_tree t, size_t first, size_t count, float* out);
+/* Dirty-world bits of the last compute (the EventWorldMatricesChanged payload). */
+int dpcull_tree_dirty_world(dpcull_ctx ctx, dpcull_tree t, uint32_t* words, size_t n_words);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* DPCULL_H */

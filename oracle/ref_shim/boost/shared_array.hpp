@@ -1,0 +1,2 @@
+#pragma once
+// Empty stand-in: the culling and transform sources include this header but use nothing from it.

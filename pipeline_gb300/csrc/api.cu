@@ -1,0 +1,1486 @@
+// api.cu -- the C ABI (include/dpcull.h) over the GB300 culling kernels.
+//
+// Host-side bookkeeping mirrors the reference's state classes:
+//   * Group  ~ GroupBitSet (dp/culling/GroupBitSet.h:40-104): object count, incarnation
+//     (bumped on every add / remove), matrices; objects and matrices live in HBM.
+//   * Result ~ ResultBitSet (dp/culling/ResultBitSet.h:38-67): visibility bits sized
+//     lazily at cull time when the group's incarnation changed, new bits visible.
+//   * Tree   ~ dp::transform::Tree (dp/transform/Tree.h:42-129): the level lists are
+//     kept as hazard-free segments, matrices and dirty bits live in HBM.
+// Indices are validated on the host before any launch (a bad transform index is an
+// error code, never a device fault); kernels check again and raise an error bit.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cerrno>
+#include <cfloat>
+#include <chrono>
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <map>
+#include <string>
+#include <vector>
+
+#include <sys/stat.h>
+
+#include "../../include/dpcull.h"
+#include "dpcull_internal.h"
+
+using namespace dpcull;
+
+namespace {
+
+thread_local std::string g_last_error;
+
+int fail(int code, const char* fmt, ...)
+{
+  char buf[512];
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(buf, sizeof buf, fmt, ap);
+  va_end(ap);
+  g_last_error = buf;
+  return code;
+}
+
+int cuda_fail(cudaError_t e, const char* what)
+{
+  return fail(DPCULL_ERR_CUDA, "%s: %s", what, cudaGetErrorString(e));
+}
+
+#define CU(call)                                        \
+  do {                                                  \
+    cudaError_t e_ = (call);                            \
+    if (e_ != cudaSuccess) return cuda_fail(e_, #call); \
+  } while (0)
+
+size_t round_up(size_t x, size_t m) { return (x + m - 1) / m * m; }
+uint32_t tiles_of(size_t n) { return (uint32_t)((n + kTileObjects - 1) / kTileObjects); }
+
+struct Group {
+  bool alive = false;
+  size_t n = 0, cap = 0;
+  float* soa = nullptr;             // 7 rows x cap
+  std::vector<uint32_t> xform;      // host mirror of transform indices (validation)
+  uint32_t max_xform = 0;
+  bool max_dirty = false;
+  float* mats = nullptr;
+  size_t n_mats = 0, mats_cap = 0;  // mats_cap = 0 for bound (not owned) matrices
+  uint64_t incarnation = 0;
+  std::vector<uint32_t> results;
+  float* box_scratch = nullptr;     // partials + counter + output
+};
+
+struct Result {
+  bool alive = false;
+  uint32_t group = 0;
+  size_t size_bits = 0;             // ResultBitSet::m_results.getSize()
+  uint64_t incarnation = ~0ull;     // ResultBitSet.cpp:43
+  uint32_t* bits = nullptr;
+  size_t words_cap = 0;
+  uint32_t* changed = nullptr;
+  size_t changed_cap = 0;
+  uint32_t* n_changed = nullptr;
+  unsigned long long* status = nullptr;
+  size_t status_cap = 0;
+};
+
+struct TreeLaunch {
+  bool single_cta;
+  uint32_t a, b;  // segment range (single CTA) or entry range (grid)
+};
+
+struct Tree {
+  bool alive = false;
+  size_t cap = 0, words = 0;
+  float* local = nullptr;
+  float* world = nullptr;
+  uint32_t* dirty_local = nullptr;
+  uint32_t* dirty_world = nullptr;
+  uint2* entries = nullptr;
+  size_t entries_cap = 0;
+  uint32_t* seg = nullptr;
+  size_t seg_cap = 0;
+  std::vector<TreeLaunch> schedule;
+};
+
+struct Plan {
+  bool alive = false;
+  std::vector<uint32_t> groups;
+  std::vector<uint64_t> incarnations;
+  std::vector<uint32_t> results;
+  std::vector<CullScene> scenes;
+  std::vector<CullView> views;
+  CullScene* d_scenes = nullptr;
+  CullView* d_views = nullptr;
+  CullView* h_views[2] = {nullptr, nullptr};   // pinned, double buffered
+  cudaGraphExec_t exec[2] = {nullptr, nullptr};
+  cudaEvent_t done[2] = {nullptr, nullptr};
+  bool pending[2] = {false, false};
+  bool fresh[2] = {false, false};      // slot holds matrices from set_views
+  std::vector<uint32_t> all_groups;    // every job's group (empty ones included)
+  std::vector<uint64_t> all_incarnations;
+  int next = 0;
+  dpcull_tuning tuning{};
+  uint32_t n_items = 0;
+  int grid = 0;
+};
+
+}  // namespace
+
+struct dpcull_ctx_s {
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  bool own_stream = false;
+  CullControl* ctl = nullptr;
+  unsigned int* h_err = nullptr;     // pinned copy of ctl->error / error_info
+  int sm_count = 0;
+  uint64_t launches = 0;
+  uint64_t device_bytes = 0;
+  std::vector<Group> groups;
+  std::vector<Result> results;
+  std::vector<Tree> trees;
+  std::vector<Plan> plans;
+  std::map<std::string, dpcull_tuning> tune_cache;
+};
+
+namespace {
+
+int dalloc(dpcull_ctx c, void** p, size_t bytes)
+{
+  *p = nullptr;
+  if (!bytes) return DPCULL_OK;
+  cudaError_t e = cudaMalloc(p, bytes);
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    return fail(DPCULL_ERR_NO_MEMORY, "cudaMalloc(%zu bytes): %s", bytes, cudaGetErrorString(e));
+  }
+  c->device_bytes += bytes;
+  return DPCULL_OK;
+}
+
+void dfree(dpcull_ctx c, void* p, size_t bytes)
+{
+  if (p) {
+    cudaFree(p);
+    c->device_bytes -= bytes;
+  }
+}
+
+Group* get_group(dpcull_ctx c, dpcull_group g)
+{
+  if (!c || g >= c->groups.size() || !c->groups[g].alive) return nullptr;
+  return &c->groups[g];
+}
+
+Result* get_result(dpcull_ctx c, dpcull_result r)
+{
+  if (!c || r >= c->results.size() || !c->results[r].alive) return nullptr;
+  return &c->results[r];
+}
+
+Tree* get_tree(dpcull_ctx c, dpcull_tree t)
+{
+  if (!c || t >= c->trees.size() || !c->trees[t].alive) return nullptr;
+  return &c->trees[t];
+}
+
+Plan* get_plan(dpcull_ctx c, dpcull_plan p)
+{
+  if (!c || p >= c->plans.size() || !c->plans[p].alive) return nullptr;
+  return &c->plans[p];
+}
+
+size_t soa_bytes(size_t cap) { return 7 * cap * sizeof(float); }
+
+// Grows the SoA block to hold n objects (copying the existing rows).
+int group_reserve(dpcull_ctx c, Group& g, size_t n)
+{
+  if (n <= g.cap && g.soa) return DPCULL_OK;
+  size_t cap = round_up(std::max<size_t>(n, 1), kTileObjects);
+  if (g.cap) cap = std::max(cap, round_up(g.cap + g.cap / 2, kTileObjects));
+  float* soa = nullptr;
+  int rc = dalloc(c, (void**)&soa, soa_bytes(cap));
+  if (rc) return rc;
+  CU(cudaMemsetAsync(soa, 0, soa_bytes(cap), c->stream));
+  if (g.soa && g.n)
+    for (int r = 0; r < 7; ++r)
+      CU(cudaMemcpyAsync(soa + (size_t)r * cap, g.soa + (size_t)r * g.cap, g.n * sizeof(float),
+                         cudaMemcpyDeviceToDevice, c->stream));
+  if (g.soa) {
+    CU(cudaStreamSynchronize(c->stream));
+    dfree(c, g.soa, soa_bytes(g.cap));
+  }
+  g.soa = soa;
+  g.cap = cap;
+  return DPCULL_OK;
+}
+
+// Uploads k planar objects into rows starting at object `at` (contiguous).
+int upload_rows(dpcull_ctx c, Group& g, size_t at, size_t k, const float* lower,
+                const float* extent, const uint32_t* xform)
+{
+  if (!k) return DPCULL_OK;
+  for (int r = 0; r < 3; ++r) {
+    CU(cudaMemcpyAsync(g.soa + (size_t)r * g.cap + at, lower + (size_t)r * k, k * sizeof(float),
+                       cudaMemcpyHostToDevice, c->stream));
+    CU(cudaMemcpyAsync(g.soa + (size_t)(3 + r) * g.cap + at, extent + (size_t)r * k,
+                       k * sizeof(float), cudaMemcpyHostToDevice, c->stream));
+  }
+  CU(cudaMemcpyAsync(g.soa + (size_t)6 * g.cap + at, xform, k * sizeof(uint32_t),
+                     cudaMemcpyHostToDevice, c->stream));
+  return DPCULL_OK;
+}
+
+uint32_t group_max_xform(Group& g)
+{
+  if (g.max_dirty) {
+    uint32_t m = 0;
+    for (size_t i = 0; i < g.n; ++i) m = std::max(m, g.xform[i]);
+    g.max_xform = m;
+    g.max_dirty = false;
+  }
+  return g.max_xform;
+}
+
+int check_cull_ready(Group& g)
+{
+  if (g.n > kMaxObjects) return fail(DPCULL_ERR_INVALID_ARGUMENT, "group has %zu objects (max %u)", g.n, kMaxObjects);
+  if (g.n && !g.mats) return fail(DPCULL_ERR_STATE, "group has objects but no matrices");
+  if (g.n && group_max_xform(g) >= g.n_mats)
+    return fail(DPCULL_ERR_OUT_OF_RANGE, "transform index %u >= matrix count %zu", group_max_xform(g),
+                g.n_mats);
+  return DPCULL_OK;
+}
+
+__global__ void resize_bits_kernel(uint32_t* bits, size_t old_bits, size_t new_bits, size_t words)
+{
+  // ResultBitSet.cpp:65-79: keep [0, min(old,new)), set [old, new) visible, clear >= new.
+  for (size_t w = blockIdx.x * (size_t)blockDim.x + threadIdx.x; w < words;
+       w += (size_t)gridDim.x * blockDim.x) {
+    uint32_t v = bits[w];
+    for (int b = 0; b < 32; ++b) {
+      const size_t i = w * 32 + b;
+      if (i >= new_bits) v &= ~(1u << b);
+      else if (i >= old_bits) v |= 1u << b;
+    }
+    bits[w] = v;
+  }
+}
+
+// Capacity for a group of n objects, and the ResultBitSet resize on incarnation change.
+int result_prepare(dpcull_ctx c, Result& r, Group& g)
+{
+  const uint32_t tiles = tiles_of(g.n);
+  const size_t words = std::max<size_t>((size_t)tiles * kTileWords, 32);
+  if (words > r.words_cap) {
+    uint32_t* nb = nullptr;
+    int rc = dalloc(c, (void**)&nb, words * 4);
+    if (rc) return rc;
+    CU(cudaMemsetAsync(nb, 0, words * 4, c->stream));
+    if (r.bits) {
+      CU(cudaMemcpyAsync(nb, r.bits, r.words_cap * 4, cudaMemcpyDeviceToDevice, c->stream));
+      CU(cudaStreamSynchronize(c->stream));
+      dfree(c, r.bits, r.words_cap * 4);
+    }
+    r.bits = nb;
+    r.words_cap = words;
+  }
+  const size_t chcap = std::max<size_t>(g.n, 1);
+  if (chcap > r.changed_cap) {
+    CU(cudaStreamSynchronize(c->stream));
+    dfree(c, r.changed, r.changed_cap * 4);
+    r.changed = nullptr;
+    size_t want = std::max(chcap, r.changed_cap + r.changed_cap / 2);
+    int rc = dalloc(c, (void**)&r.changed, want * 4);
+    if (rc) return rc;
+    r.changed_cap = want;
+  }
+  if (std::max<size_t>(tiles, 1) > r.status_cap) {
+    CU(cudaStreamSynchronize(c->stream));
+    dfree(c, r.status, r.status_cap * 8);
+    r.status = nullptr;
+    size_t want = std::max<size_t>(tiles, r.status_cap + r.status_cap / 2);
+    int rc = dalloc(c, (void**)&r.status, want * 8);
+    if (rc) return rc;
+    CU(cudaMemsetAsync(r.status, 0, want * 8, c->stream));
+    r.status_cap = want;
+  }
+  if (r.incarnation != g.incarnation) {
+    r.incarnation = g.incarnation;
+    const size_t old = r.size_bits;
+    r.size_bits = g.n;
+    resize_bits_kernel<<<(unsigned)std::min<size_t>((r.words_cap + 255) / 256, 4096), 256, 0,
+                         c->stream>>>(r.bits, old, g.n, r.words_cap);
+    CU(cudaGetLastError());
+    c->launches++;
+  }
+  return DPCULL_OK;
+}
+
+CullScene scene_of(Group& g, uint32_t view_begin, uint32_t n_views, uint32_t vpp,
+                   uint32_t item_begin)
+{
+  CullScene s{};
+  s.soa = g.soa;
+  s.mats = g.mats;
+  s.cap = (uint32_t)g.cap;
+  s.n_objects = (uint32_t)g.n;
+  s.n_mats = (uint32_t)std::min<size_t>(g.n_mats, 0xFFFFFFFFu);
+  s.view_begin = view_begin;
+  s.n_views = n_views;
+  s.n_vgroups = (n_views + vpp - 1) / vpp;
+  s.n_tiles = tiles_of(g.n);
+  s.item_begin = item_begin;
+  return s;
+}
+
+CullView view_of(Result& r, const float* vp)
+{
+  CullView v{};
+  memcpy(v.vp, vp, sizeof v.vp);
+  v.bits = r.bits;
+  v.changed = r.changed;
+  v.n_changed = r.n_changed;
+  v.status = r.status;
+  return v;
+}
+
+int check_device_errors(dpcull_ctx c)
+{
+  CU(cudaMemcpyAsync(c->h_err, &c->ctl->error, 2 * sizeof(unsigned int), cudaMemcpyDeviceToHost,
+                     c->stream));
+  CU(cudaStreamSynchronize(c->stream));
+  const unsigned int err = c->h_err[0], info = c->h_err[1];
+  if (err) {
+    CU(cudaMemsetAsync(&c->ctl->error, 0, 2 * sizeof(unsigned int), c->stream));
+    CU(cudaStreamSynchronize(c->stream));
+    if (err & kErrLookbackTimeout)
+      return fail(DPCULL_ERR_TIMEOUT, "a look-back wait expired on the device");
+    if (err & kErrBadTransform)
+      return fail(DPCULL_ERR_OUT_OF_RANGE, "object %u has a transform index past the matrix array", info);
+  }
+  return DPCULL_OK;
+}
+
+// Look-back poll budget: 2^20 polls with a 64 ns back-off, well under a second.  A tile
+// normally waits for a predecessor that is already running, a few microseconds at most.
+uint32_t spin_limit() { return 1u << 20; }
+
+int default_vpp(uint32_t max_views)
+{
+  return max_views <= 1 ? 1 : max_views <= 2 ? 2 : max_views <= 4 ? 4 : 8;
+}
+
+// Builds scenes/views for a job list; returns n_items.
+int build_batch(dpcull_ctx c, const dpcull_job* jobs, size_t n_jobs, uint32_t vpp,
+                std::vector<CullScene>& scenes, std::vector<CullView>& views, uint32_t* n_items,
+                std::vector<uint32_t>* groups_out, std::vector<uint32_t>* results_out)
+{
+  scenes.clear();
+  views.clear();
+  uint32_t items = 0;
+  for (size_t j = 0; j < n_jobs; ++j) {
+    Group* g = get_group(c, jobs[j].group);
+    if (!g) return fail(DPCULL_ERR_INVALID_ARGUMENT, "job %zu: bad group", j);
+    if (!jobs[j].n_views || !jobs[j].results || !jobs[j].vps)
+      return fail(DPCULL_ERR_INVALID_ARGUMENT, "job %zu: needs views, results and matrices", j);
+    int rc = check_cull_ready(*g);
+    if (rc) return rc;
+    if (g->n == 0) {
+      for (uint32_t v = 0; v < jobs[j].n_views; ++v) {
+        Result* r = get_result(c, jobs[j].results[v]);
+        if (!r || r->group != jobs[j].group) return fail(DPCULL_ERR_INVALID_ARGUMENT, "job %zu: bad result", j);
+        rc = result_prepare(c, *r, *g);
+        if (rc) return rc;
+        CU(cudaMemsetAsync(r->n_changed, 0, 4, c->stream));
+      }
+      continue;
+    }
+    const uint32_t vb = (uint32_t)views.size();
+    for (uint32_t v = 0; v < jobs[j].n_views; ++v) {
+      Result* r = get_result(c, jobs[j].results[v]);
+      if (!r || r->group != jobs[j].group) return fail(DPCULL_ERR_INVALID_ARGUMENT, "job %zu: bad result", j);
+      rc = result_prepare(c, *r, *g);
+      if (rc) return rc;
+      views.push_back(view_of(*r, jobs[j].vps + 16 * (size_t)v));
+      if (results_out) results_out->push_back(jobs[j].results[v]);
+    }
+    CullScene s = scene_of(*g, vb, jobs[j].n_views, vpp, items);
+    items += s.n_tiles * s.n_vgroups;
+    scenes.push_back(s);
+    if (groups_out) groups_out->push_back(jobs[j].group);
+  }
+  *n_items = items;
+  return DPCULL_OK;
+}
+
+int persistent_grid(dpcull_ctx c, uint32_t vpp, uint32_t ctas_per_sm, uint32_t n_items,
+                    uint32_t per_ticket)
+{
+  int occ = cull_max_ctas_per_sm((int)vpp);
+  int per_sm = ctas_per_sm ? std::min<int>((int)ctas_per_sm, occ) : occ;
+  long long want = ((long long)n_items + per_ticket - 1) / per_ticket;
+  long long grid = std::min<long long>((long long)c->sm_count * per_sm, want);
+  return (int)std::max<long long>(grid, 1);
+}
+
+int launch_batch(dpcull_ctx c, const CullScene* d_scenes, const CullView* d_views,
+                 uint32_t n_scenes, uint32_t n_items, const dpcull_tuning& t, cudaStream_t s)
+{
+  CullLaunch a{};
+  a.scenes = d_scenes;
+  a.views = d_views;
+  a.n_scenes = n_scenes;
+  a.n_items = n_items;
+  a.items_per_ticket = std::max<uint32_t>(1, t.tiles_per_ticket);
+  a.spin_limit = spin_limit();
+  a.ctl = c->ctl;
+  const int grid = persistent_grid(c, t.views_per_pass, t.ctas_per_sm, n_items, a.items_per_ticket);
+  if (launch_cull(a, grid, (int)t.views_per_pass, s)) return cuda_fail(cudaGetLastError(), "cull launch");
+  c->launches++;
+  return DPCULL_OK;
+}
+
+bool valid_vpp(uint32_t v) { return v == 1 || v == 2 || v == 4 || v == 8; }
+
+std::string tune_key(const std::vector<CullScene>& scenes, const std::vector<CullView>& views)
+{
+  uint64_t objs = 0;
+  uint32_t maxv = 0;
+  for (auto& s : scenes) {
+    objs += s.n_objects;
+    maxv = std::max(maxv, s.n_views);
+  }
+  const int bucket = objs ? (int)std::floor(std::log2((double)objs)) : 0;
+  char buf[96];
+  snprintf(buf, sizeof buf, "n2^%d_v%zu_maxv%u_s%zu", bucket, views.size(), maxv, scenes.size());
+  return buf;
+}
+
+std::string tune_cache_path()
+{
+  const char* p = getenv("DPCULL_TUNE_CACHE");
+  if (p && *p) return p;
+  const char* home = getenv("HOME");
+  return std::string(home && *home ? home : "/tmp") + "/.cache/dpcull_tune.json";
+}
+
+void tune_cache_load(dpcull_ctx c)
+{
+  FILE* f = fopen(tune_cache_path().c_str(), "r");
+  if (!f) return;
+  char line[512];
+  while (fgets(line, sizeof line, f)) {
+    char key[128];
+    unsigned a, b, d;
+    // one JSON object per line: {"key": "...", "views_per_pass": a, "tiles_per_ticket": b, "ctas_per_sm": d}
+    if (sscanf(line, " {\"key\": \"%127[^\"]\", \"views_per_pass\": %u, \"tiles_per_ticket\": %u, \"ctas_per_sm\": %u",
+               key, &a, &b, &d) == 4 && valid_vpp(a))
+      c->tune_cache[key] = dpcull_tuning{a, b, d, 0};
+  }
+  fclose(f);
+}
+
+void tune_cache_store(const std::string& key, const dpcull_tuning& t)
+{
+  std::string path = tune_cache_path();
+  const size_t slash = path.find_last_of('/');
+  if (slash != std::string::npos && slash > 0) mkdir(path.substr(0, slash).c_str(), 0755);
+  FILE* f = fopen(path.c_str(), "a");
+  if (!f) return;
+  fprintf(f, "{\"key\": \"%s\", \"views_per_pass\": %u, \"tiles_per_ticket\": %u, \"ctas_per_sm\": %u}\n",
+          key.c_str(), t.views_per_pass, t.tiles_per_ticket, t.ctas_per_sm);
+  fclose(f);
+}
+
+}  // namespace
+
+// ===================================================================================
+extern "C" {
+
+const char* dpcull_last_error(void) { return g_last_error.c_str(); }
+uint32_t dpcull_version(void) { return (1u << 16) | 0u; }
+
+int dpcull_ctx_create(int device, void* stream, dpcull_ctx* out)
+{
+  if (!out) return fail(DPCULL_ERR_INVALID_ARGUMENT, "out is null");
+  *out = nullptr;
+  int n = 0;
+  cudaError_t e = cudaGetDeviceCount(&n);
+  if (e != cudaSuccess || n == 0) {
+    cudaGetLastError();
+    return fail(DPCULL_ERR_CUDA, "no CUDA device available (%s)", cudaGetErrorString(e));
+  }
+  if (device < 0 || device >= n) return fail(DPCULL_ERR_INVALID_ARGUMENT, "device %d of %d", device, n);
+  CU(cudaSetDevice(device));
+  dpcull_ctx c = new dpcull_ctx_s();
+  c->device = device;
+  if (stream) {
+    c->stream = static_cast<cudaStream_t>(stream);
+  } else {
+    e = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking);
+    if (e != cudaSuccess) {
+      delete c;
+      return cuda_fail(e, "cudaStreamCreate");
+    }
+    c->own_stream = true;
+  }
+  cudaDeviceGetAttribute(&c->sm_count, cudaDevAttrMultiProcessorCount, device);
+  int rc = dalloc(c, (void**)&c->ctl, sizeof(CullControl));
+  if (rc) {
+    delete c;
+    return rc;
+  }
+  CullControl init{};
+  init.epoch = 1;
+  init.stride = 1;
+  e = cudaMemcpy(c->ctl, &init, sizeof init, cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) e = cudaMallocHost((void**)&c->h_err, 2 * sizeof(unsigned int));
+  if (e != cudaSuccess) {
+    dpcull_ctx_destroy(c);
+    return cuda_fail(e, "context set-up");
+  }
+  tune_cache_load(c);
+  *out = c;
+  return DPCULL_OK;
+}
+
+int dpcull_ctx_destroy(dpcull_ctx c)
+{
+  if (!c) return fail(DPCULL_ERR_INVALID_ARGUMENT, "null context");
+  cudaSetDevice(c->device);
+  cudaStreamSynchronize(c->stream);
+  for (dpcull_plan p = 0; p < c->plans.size(); ++p)
+    if (c->plans[p].alive) dpcull_plan_destroy(c, p);
+  for (dpcull_tree t = 0; t < c->trees.size(); ++t)
+    if (c->trees[t].alive) dpcull_tree_destroy(c, t);
+  for (dpcull_result r = 0; r < c->results.size(); ++r)
+    if (c->results[r].alive) dpcull_result_destroy(c, r);
+  for (dpcull_group g = 0; g < c->groups.size(); ++g)
+    if (c->groups[g].alive) dpcull_group_destroy(c, g);
+  if (c->ctl) cudaFree(c->ctl);
+  if (c->h_err) cudaFreeHost(c->h_err);
+  if (c->own_stream) cudaStreamDestroy(c->stream);
+  delete c;
+  return DPCULL_OK;
+}
+
+int dpcull_ctx_synchronize(dpcull_ctx c)
+{
+  if (!c) return fail(DPCULL_ERR_INVALID_ARGUMENT, "null context");
+  CU(cudaStreamSynchronize(c->stream));
+  return check_device_errors(c);
+}
+
+void* dpcull_ctx_stream(dpcull_ctx c) { return c ? (void*)c->stream : nullptr; }
+uint64_t dpcull_ctx_kernel_launches(dpcull_ctx c) { return c ? c->launches : 0; }
+uint64_t dpcull_ctx_device_bytes(dpcull_ctx c) { return c ? c->device_bytes : 0; }
+
+// ---- groups ------------------------------------------------------------------------
+int dpcull_group_create(dpcull_ctx c, dpcull_group* out)
+{
+  if (!c || !out) return fail(DPCULL_ERR_INVALID_ARGUMENT, "null argument");
+  c->groups.emplace_back();
+  Group& g = c->groups.back();
+  g.alive = true;
+  int rc = dalloc(c, (void**)&g.box_scratch, (bbox_partials_needed(0) + 16) * sizeof(float));
+  if (rc) {
+    g.alive = false;
+    return rc;
+  }
+  CU(cudaMemsetAsync(g.box_scratch, 0, (bbox_partials_needed(0) + 16) * sizeof(float), c->stream));
+  *out = (dpcull_group)(c->groups.size() - 1);
+  return DPCULL_OK;
+}
+
+int dpcull_group_destroy(dpcull_ctx c, dpcull_group gh)
+{
+  Group* g = get_group(c, gh);
+  if (!g) return fail(DPCULL_ERR_INVALID_ARGUMENT, "bad group %u", gh);
+  cudaStreamSynchronize(c->stream);
+  for (uint32_t r : g->results)
+    if (get_result(c, r)) dpcull_result_destroy(c, r);
+  dfree(c, g->soa, soa_bytes(g->cap));
+  if (g->mats_cap) dfree(c, g->mats, g->mats_cap * 64);
+  dfree(c, g->box_scratch, (bbox_partials_needed(0) + 16) * sizeof(float));
+  *g = Group();
+  return DPCULL_OK;
+}
+
+int dpcull_group_set_objects(dpcull_ctx c, dpcull_group gh, size_t n, const float* lower,
+                             const float* extent, const uint32_t* xform)
+{
+  Group* g = get_group(c, gh);
+  if (!g) return fail(DPCULL_ERR_INVALID_ARGUMENT, "bad group %u", gh);
+  if (n && (!lower || !extent || !xform)) return fail(DPCULL_ERR_INVALID_ARGUMENT, "null object arrays");
+  if (n > kMaxObjects) return fail(DPCULL_ERR_INVALID_ARGUMENT, "%zu objects (max %u)", n, kMaxObjects);
+  int rc = group_reserve(c, *g, n);
+  if (rc) return rc;
+  // Rows past the new count must read as zero (padding of the last tile).
+  if (n < g->n)
+    for (int r = 0; r < 7; ++r)
+      CU(cudaMemsetAsync(g->soa + (size_t)r * g->cap + n, 0, (g->n - n) * sizeof(float), c->stream));
+  rc = upload_rows(c, *g, 0, n, lower, extent, xform);
+  if (rc) return rc;
+  g->xform.assign(xform, xform + n);
+  g->max_dirty = true;
+  g->n = n;
+  g->incarnation += n ? n : 1;  // clearObjects + addObject x n
+  CU(cudaStreamSynchronize(c->stream));
+  return DPCULL_OK;
+}
+
+int dpcull_group_append_objects(dpcull_ctx c, dpcull_group gh, size_t k, const float* lower,
+                                const float* extent, const uint32_t* xform)
+{
+  Group* g = get_group(c, gh);
+  if (!g) return fail(DPCULL_ERR_INVALID_ARGUMENT, "bad group %u", gh);
+  if (!k) return DPCULL_OK;
+  if (!lower || !extent || !xform) return fail(DPCULL_ERR_INVALID_ARGUMENT, "null object arrays");
+  if (g->n + k > kMaxObjects) return fail(DPCULL_ERR_INVALID_ARGUMENT, "too many objects");
+  int rc = group_reserve(c, *g, g->n + k);
+  if (rc) return rc;
+  rc = upload_rows(c, *g, g->n, k, lower, extent, xform);
+  if (rc) return rc;
+  g->xform.insert(g->xform.end(), xform, xform + k);
+  for (size_t i = 0; i < k; ++i) g->max_xform = std::max(g->max_xform, xform[i]);
+  g->n += k;
+  g->incarnation += k;
+  CU(cudaStreamSynchronize(c->stream));
+  return DPCULL_OK;
+}
+
+int dpcull_group_update_objects(dpcull_ctx c, dpcull_group gh, size_t k, const uint32_t* index,
+                                const float* lower, const float* extent, const uint32_t* xform)
+{
+  Group* g = get_group(c, gh);
+  if (!g) return fail(DPCULL_ERR_INVALID_ARGUMENT, "bad group %u", gh);
+  if (!k) return DPCULL_OK;
+  if (!index || !lower || !extent || !xform) return fail(DPCULL_ERR_INVALID_ARGUMENT, "null arrays");
+  for (size_t i = 0; i < k; ++i)
+    if (index[i] >= g->n) return fail(DPCULL_ERR_OUT_OF_RANGE, "object index %u >= %zu", index[i], g->n);
+  std::vector<float> rows(7 * k);
+  for (int r = 0; r < 3; ++r) {
+    memcpy(&rows[r * k], lower + r * k, k * 4);
+    memcpy(&rows[(3 + r) * k], extent + r * k, k * 4);
+  }
+  memcpy(&rows[6 * k], xform, k * 4);
+  float* d = nullptr;
+  uint32_t* di = nullptr;
+  int rc = dalloc(c, (void**)&d, rows.size() * 4);
+  if (rc) return rc;
+  rc = dalloc(c, (void**)&di, k * 4);
+  if (rc) {
+    dfree(c, d, rows.size() * 4);
+    return rc;
+  }
+  cudaMemcpyAsync(d, rows.data(), rows.size() * 4, cudaMemcpyHostToDevice, c->stream);
+  cudaMemcpyAsync(di, index, k * 4, cudaMemcpyHostToDevice, c->stream);
+  launch_scatter_objects(g->soa, (uint32_t)g->cap, d, di, (uint32_t)k, c->stream);
+  c->launches++;
+  cudaError_t e = cudaStreamSynchronize(c->stream);
+  dfree(c, d, rows.size() * 4);
+  dfree(c, di, k * 4);
+  if (e != cudaSuccess) return cuda_fail(e, "update objects");
+  for (size_t i = 0; i < k; ++i) g->xform[index[i]] = xform[i];
+  g->max_dirty = true;
+  return DPCULL_OK;
+}
+
+int dpcull_group_remove_object(dpcull_ctx c, dpcull_group gh, size_t index)
+{
+  Group* g = get_group(c, gh);
+  if (!g) return fail(DPCULL_ERR_INVALID_ARGUMENT, "bad group %u", gh);
+  if (index >= g->n) return fail(DPCULL_ERR_STATE, "object does not belong to this group");
+  const size_t last = g->n - 1;
+  if (index != last) {
+    if (launch_move_object(g->soa, (uint32_t)g->cap, (uint32_t)last, (uint32_t)index, c->stream))
+      return cuda_fail(cudaGetLastError(), "move object");
+    c->launches++;
+    g->xform[index] = g->xform[last];
+  }
+  for (int r = 0; r < 7; ++r)
+    CU(cudaMemsetAsync(g->soa + (size_t)r * g->cap + last, 0, sizeof(float), c->stream));
+  g->xform.pop_back();
+  g->max_dirty = true;
+  g->n = last;
+  // Event(old = new size, new = hole) to every result (GroupBitSet.cpp:108).
+  for (uint32_t rh : g->results) {
+    Result* r = get_result(c, rh);
+    if (!r || !r->bits) continue;
+    if (launch_move_bit(r->bits, (uint32_t)r->size_bits, (uint32_t)g->n, (uint32_t)index, c->stream))
+      return cuda_fail(cudaGetLastError(), "move bit");
+    c->launches++;
+  }
+  g->incarnation++;
+  return DPCULL_OK;
+}
+
+int dpcull_group_count(dpcull_ctx c, dpcull_group gh, size_t* n)
+{
+  Group* g = get_group(c, gh);
+  if (!g || !n) return fail(DPCULL_ERR_INVALID_ARGUMENT, "bad group %u", gh);
+  *n = g->n;
+  return DPCULL_OK;
+}
+
+static int ensure_owned_mats(dpcull_ctx c, Group& g, size_t count)
+{
+  if (g.mats_cap >= count && g.mats_cap) return DPCULL_OK;
+  CU(cudaStreamSynchronize(c->stream));
+  if (g.mats_cap) dfree(c, g.mats, g.mats_cap * 64);
+  g.mats = nullptr;
+  g.mats_cap = 0;
+  const size_t cap = std::max<size_t>(count, 1);
+  int rc = dalloc(c, (void**)&g.mats, cap * 64);
+  if (rc) return rc;
+  g.mats_cap = cap;
+  return DPCULL_OK;
+}
+
+int dpcull_group_set_matrices(dpcull_ctx c, dpcull_group gh, const void* matrices, size_t count,
+                              size_t stride)
+{
+  Group* g = get_group(c, gh);
+  if (!g) return fail(DPCULL_ERR_INVALID_ARGUMENT, "bad group %u", gh);
+  if (count && (!matrices || stride < 64)) return fail(DPCULL_ERR_INVALID_ARGUMENT, "bad matrix array");
+  if (count > 0xFFFFFFFFull) return fail(DPCULL_ERR_INVALID_ARGUMENT, "too many matrices");
+  int rc = ensure_owned_mats(c, *g, count);
+  if (rc) return rc;
+  if (count) {
+    if (stride == 64) {
+      CU(cudaMemcpyAsync(g->mats, matrices, count * 64, cudaMemcpyHostToDevice, c->stream));
+    } else {
+      CU(cudaMemcpy2DAsync(g->mats, 64, matrices, stride, 64, count, cudaMemcpyHostToDevice, c->stream));
+    }
+  }
+  g->n_mats = count;
+  CU(cudaStreamSynchronize(c->stream));
+  return DPCULL_OK;
+}
+
+int dpcull_group_update_matrices(dpcull_ctx c, dpcull_group gh, size_t k, const uint32_t* index,
+                                 const void* matrices, size_t stride)
+{
+  Group* g = get_group(c, gh);
+  if (!g) return fail(DPCULL_ERR_INVALID_ARGUMENT, "bad group %u", gh);
+  if (!k) return DPCULL_OK;
+  if (!index || !matrices || stride < 64) return fail(DPCULL_ERR_INVALID_ARGUMENT, "bad arguments");
+  if (!g->mats_cap) return fail(DPCULL_ERR_STATE, "group matrices are bound, not owned");
+  std::vector<float> packed(16 * k);
+  for (size_t i = 0; i < k; ++i) {
+    if (index[i] >= g->n_mats) return fail(DPCULL_ERR_OUT_OF_RANGE, "matrix %u >= %zu", index[i], g->n_mats);
+    memcpy(&packed[16 * i], (const char*)matrices + (size_t)index[i] * stride, 64);
+  }
+  float* d = nullptr;
+  uint32_t* di = nullptr;
+  int rc = dalloc(c, (void**)&d, 64 * k);
+  if (rc) return rc;
+  rc = dalloc(c, (void**)&di, 4 * k);
+  if (rc) {
+    dfree(c, d, 64 * k);
+    return rc;
+  }
+  cudaMemcpyAsync(d, packed.data(), 64 * k, cudaMemcpyHostToDevice, c->stream);
+  cudaMemcpyAsync(di, index, 4 * k, cudaMemcpyHostToDevice, c->stream);
+  launch_scatter_matrices(g->mats, d, di, (uint32_t)k, nullptr, c->stream);
+  c->launches++;
+  cudaError_t e = cudaStreamSynchronize(c->stream);
+  dfree(c, d, 64 * k);
+  dfree(c, di, 4 * k);
+  if (e != cudaSuccess) return cuda_fail(e, "update matrices");
+  return DPCULL_OK;
+}
+
+int dpcull_group_bind_device_matrices(dpcull_ctx c, dpcull_group gh, const float* dev, size_t count)
+{
+  Group* g = get_group(c, gh);
+  if (!g) return fail(DPCULL_ERR_INVALID_ARGUMENT, "bad group %u", gh);
+  if (count && (!dev || ((uintptr_t)dev & 15))) return fail(DPCULL_ERR_INVALID_ARGUMENT, "device matrices must be 16-byte aligned");
+  CU(cudaStreamSynchronize(c->stream));
+  if (g->mats_cap) dfree(c, g->mats, g->mats_cap * 64);
+  g->mats = const_cast<float*>(dev);
+  g->mats_cap = 0;
+  g->n_mats = count;
+  return DPCULL_OK;
+}
+
+int dpcull_group_bounding_box(dpcull_ctx c, dpcull_group gh, float lower[3], float upper[3])
+{
+  Group* g = get_group(c, gh);
+  if (!g || !lower || !upper) return fail(DPCULL_ERR_INVALID_ARGUMENT, "bad arguments");
+  float box[8] = {FLT_MAX, FLT_MAX, FLT_MAX, -FLT_MAX, -FLT_MAX, -FLT_MAX, 0, 0};
+  if (g->n) {
+    int rc = check_cull_ready(*g);
+    if (rc) return rc;
+    float* partials = g->box_scratch;
+    unsigned int* counter = reinterpret_cast<unsigned int*>(g->box_scratch + bbox_partials_needed(0));
+    float* out = g->box_scratch + bbox_partials_needed(0) + 8;
+    if (launch_bbox(g->soa, (uint32_t)g->cap, (uint32_t)g->n, g->mats, partials, counter, out, c->stream))
+      return cuda_fail(cudaGetLastError(), "bbox launch");
+    c->launches++;
+    CU(cudaMemcpyAsync(box, out, 6 * sizeof(float), cudaMemcpyDeviceToHost, c->stream));
+    CU(cudaStreamSynchronize(c->stream));
+  }
+  // Box3f(lower, upper) of the folded corners (Boxnt.h:214-231): init, then two updates.
+  for (int i = 0; i < 3; ++i) {
+    float lo = FLT_MAX, hi = -FLT_MAX;
+    const float p0 = box[i], p1 = box[3 + i];
+    if (lo > p0) lo = p0;
+    if (hi < p0) hi = p0;
+    if (lo > p1) lo = p1;
+    if (hi < p1) hi = p1;
+    lower[i] = lo;
+    upper[i] = hi;
+  }
+  return DPCULL_OK;
+}
+
+// ---- results -----------------------------------------------------------------------
+int dpcull_result_create(dpcull_ctx c, dpcull_group gh, dpcull_result* out)
+{
+  Group* g = get_group(c, gh);
+  if (!g || !out) return fail(DPCULL_ERR_INVALID_ARGUMENT, "bad group %u", gh);
+  c->results.emplace_back();
+  Result& r = c->results.back();
+  r.alive = true;
+  r.group = gh;
+  int rc = dalloc(c, (void**)&r.n_changed, 4);
+  if (rc) {
+    r.alive = false;
+    return rc;
+  }
+  CU(cudaMemsetAsync(r.n_changed, 0, 4, c->stream));
+  const dpcull_result h = (dpcull_result)(c->results.size() - 1);
+  c->groups[gh].results.push_back(h);
+  *out = h;
+  return DPCULL_OK;
+}
+
+int dpcull_result_destroy(dpcull_ctx c, dpcull_result rh)
+{
+  Result* r = get_result(c, rh);
+  if (!r) return fail(DPCULL_ERR_INVALID_ARGUMENT, "bad result %u", rh);
+  cudaStreamSynchronize(c->stream);
+  dfree(c, r->bits, r->words_cap * 4);
+  dfree(c, r->changed, r->changed_cap * 4);
+  dfree(c, r->n_changed, 4);
+  dfree(c, r->status, r->status_cap * 8);
+  if (r->group < c->groups.size()) {
+    auto& v = c->groups[r->group].results;
+    v.erase(std::remove(v.begin(), v.end(), rh), v.end());
+  }
+  *r = Result();
+  return DPCULL_OK;
+}
+
+int dpcull_cull(dpcull_ctx c, dpcull_group gh, dpcull_result rh, const float vp[16])
+{
+  Group* g = get_group(c, gh);
+  Result* r = get_result(c, rh);
+  if (!g || !r || !vp) return fail(DPCULL_ERR_INVALID_ARGUMENT, "bad group, result or matrix");
+  if (r->group != gh) return fail(DPCULL_ERR_INVALID_ARGUMENT, "result %u belongs to another group", rh);
+  int rc = check_cull_ready(*g);
+  if (rc) return rc;
+  rc = result_prepare(c, *r, *g);
+  if (rc) return rc;
+  if (g->n == 0) {
+    CU(cudaMemsetAsync(r->n_changed, 0, 4, c->stream));
+    return DPCULL_OK;
+  }
+  CullLaunch a{};
+  a.scenes = nullptr;
+  a.views = nullptr;
+  a.n_scenes = 1;
+  a.items_per_ticket = 1;
+  a.spin_limit = spin_limit();
+  a.ctl = c->ctl;
+  a.one_scene = scene_of(*g, 0, 1, 1, 0);
+  a.one_view = view_of(*r, vp);
+  a.n_items = a.one_scene.n_tiles;
+  if (launch_cull(a, (int)a.n_items, 1, c->stream)) return cuda_fail(cudaGetLastError(), "cull launch");
+  c->launches++;
+  return DPCULL_OK;
+}
+
+int dpcull_result_changed(dpcull_ctx c, dpcull_result rh, uint32_t* out, size_t cap, size_t* n)
+{
+  Result* r = get_result(c, rh);
+  if (!r || !n) return fail(DPCULL_ERR_INVALID_ARGUMENT, "bad result %u", rh);
+  uint32_t cnt = 0;
+  CU(cudaMemcpyAsync(c->h_err, r->n_changed, 4, cudaMemcpyDeviceToHost, c->stream));
+  CU(cudaStreamSynchronize(c->stream));
+  cnt = c->h_err[0];
+  int rc = check_device_errors(c);
+  if (rc) return rc;
+  *n = cnt;
+  if (cnt > cap) return fail(DPCULL_ERR_CAPACITY, "changed list has %u entries, buffer %zu", cnt, cap);
+  if (cnt) {
+    if (!out) return fail(DPCULL_ERR_INVALID_ARGUMENT, "null output");
+    CU(cudaMemcpyAsync(out, r->changed, (size_t)cnt * 4, cudaMemcpyDeviceToHost, c->stream));
+    CU(cudaStreamSynchronize(c->stream));
+  }
+  return DPCULL_OK;
+}
+
+int dpcull_result_bits(dpcull_ctx c, dpcull_result rh, uint32_t* out, size_t n_words, size_t* n_bits)
+{
+  Result* r = get_result(c, rh);
+  if (!r) return fail(DPCULL_ERR_INVALID_ARGUMENT, "bad result %u", rh);
+  const size_t words = (r->size_bits + 31) / 32;
+  if (n_bits) *n_bits = r->size_bits;
+  if (words > n_words) return fail(DPCULL_ERR_CAPACITY, "need %zu words", words);
+  if (words) {
+    if (!out) return fail(DPCULL_ERR_INVALID_ARGUMENT, "null output");
+    CU(cudaMemcpyAsync(out, r->bits, words * 4, cudaMemcpyDeviceToHost, c->stream));
+  }
+  CU(cudaStreamSynchronize(c->stream));
+  return check_device_errors(c);
+}
+
+int dpcull_result_is_visible(dpcull_ctx c, dpcull_result rh, size_t index, int* visible)
+{
+  Result* r = get_result(c, rh);
+  if (!r || !visible) return fail(DPCULL_ERR_INVALID_ARGUMENT, "bad result %u", rh);
+  if (index >= r->size_bits) {  // ResultBitSet.h:75: unknown objects are visible
+    *visible = 1;
+    return DPCULL_OK;
+  }
+  uint32_t w = 0;
+  CU(cudaMemcpyAsync(c->h_err, r->bits + index / 32, 4, cudaMemcpyDeviceToHost, c->stream));
+  CU(cudaStreamSynchronize(c->stream));
+  w = c->h_err[0];
+  *visible = (w >> (index % 32)) & 1u;
+  return DPCULL_OK;
+}
+
+int dpcull_result_device(dpcull_ctx c, dpcull_result rh, uint32_t** bits, uint32_t** changed,
+                         uint32_t** n_changed)
+{
+  Result* r = get_result(c, rh);
+  if (!r) return fail(DPCULL_ERR_INVALID_ARGUMENT, "bad result %u", rh);
+  if (bits) *bits = r->bits;
+  if (changed) *changed = r->changed;
+  if (n_changed) *n_changed = r->n_changed;
+  return DPCULL_OK;
+}
+
+// ---- batched -----------------------------------------------------------------------
+int dpcull_cull_batched(dpcull_ctx c, const dpcull_job* jobs, size_t n_jobs, const dpcull_tuning* tuning)
+{
+  if (!c || (n_jobs && !jobs)) return fail(DPCULL_ERR_INVALID_ARGUMENT, "bad arguments");
+  uint32_t maxv = 1;
+  for (size_t j = 0; j < n_jobs; ++j) maxv = std::max(maxv, jobs[j].n_views);
+  dpcull_tuning t = tuning ? *tuning : dpcull_tuning{(uint32_t)default_vpp(maxv), 1, 0, 0};
+  if (!valid_vpp(t.views_per_pass)) return fail(DPCULL_ERR_INVALID_ARGUMENT, "views_per_pass must be 1, 2, 4 or 8");
+  std::vector<CullScene> scenes;
+  std::vector<CullView> views;
+  uint32_t items = 0;
+  int rc = build_batch(c, jobs, n_jobs, t.views_per_pass, scenes, views, &items, nullptr, nullptr);
+  if (rc) return rc;
+  if (!items) return DPCULL_OK;
+  CullScene* ds = nullptr;
+  CullView* dv = nullptr;
+  rc = dalloc(c, (void**)&ds, scenes.size() * sizeof(CullScene));
+  if (rc) return rc;
+  rc = dalloc(c, (void**)&dv, views.size() * sizeof(CullView));
+  if (rc) {
+    dfree(c, ds, scenes.size() * sizeof(CullScene));
+    return rc;
+  }
+  cudaMemcpyAsync(ds, scenes.data(), scenes.size() * sizeof(CullScene), cudaMemcpyHostToDevice, c->stream);
+  cudaMemcpyAsync(dv, views.data(), views.size() * sizeof(CullView), cudaMemcpyHostToDevice, c->stream);
+  rc = launch_batch(c, ds, dv, (uint32_t)scenes.size(), items, t, c->stream);
+  cudaStreamSynchronize(c->stream);
+  dfree(c, ds, scenes.size() * sizeof(CullScene));
+  dfree(c, dv, views.size() * sizeof(CullView));
+  return rc;
+}
+
+static int plan_capture(dpcull_ctx c, Plan& p, int slot)
+{
+  cudaStream_t cs;
+  CU(cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking));
+  cudaGraph_t graph = nullptr;
+  cudaError_t e = cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal);
+  if (e == cudaSuccess)
+    e = cudaMemcpyAsync(p.d_views, p.h_views[slot], p.views.size() * sizeof(CullView),
+                        cudaMemcpyHostToDevice, cs);
+  int rc = DPCULL_OK;
+  if (e == cudaSuccess) {
+    const uint64_t before = c->launches;
+    rc = launch_batch(c, p.d_scenes, p.d_views, (uint32_t)p.scenes.size(), p.n_items, p.tuning, cs);
+    c->launches = before;  // counted when the graph is replayed
+  }
+  cudaError_t e2 = cudaStreamEndCapture(cs, &graph);
+  if (e == cudaSuccess) e = e2;
+  if (e == cudaSuccess && rc == DPCULL_OK) e = cudaGraphInstantiate(&p.exec[slot], graph, 0);
+  if (graph) cudaGraphDestroy(graph);
+  cudaStreamDestroy(cs);
+  if (rc) return rc;
+  if (e != cudaSuccess) return cuda_fail(e, "plan graph capture");
+  return DPCULL_OK;
+}
+
+static int time_batch(dpcull_ctx c, const CullScene* ds, const CullView* dv, uint32_t n_scenes,
+                      uint32_t items, const dpcull_tuning& t, int reps, float* ms)
+{
+  cudaEvent_t e0, e1;
+  CU(cudaEventCreate(&e0));
+  CU(cudaEventCreate(&e1));
+  int rc = launch_batch(c, ds, dv, n_scenes, items, t, c->stream);  // warm-up
+  if (!rc) cudaEventRecord(e0, c->stream);
+  for (int i = 0; i < reps && !rc; ++i) rc = launch_batch(c, ds, dv, n_scenes, items, t, c->stream);
+  if (!rc) {
+    cudaEventRecord(e1, c->stream);
+    cudaEventSynchronize(e1);
+    cudaEventElapsedTime(ms, e0, e1);
+    *ms /= (float)reps;
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  return rc;
+}
+
+int dpcull_autotune(dpcull_ctx c, const dpcull_job* jobs, size_t n_jobs, dpcull_tuning* out)
+{
+  if (!c || !out || (n_jobs && !jobs)) return fail(DPCULL_ERR_INVALID_ARGUMENT, "bad arguments");
+  uint32_t maxv = 1;
+  for (size_t j = 0; j < n_jobs; ++j) maxv = std::max(maxv, jobs[j].n_views);
+  // Save every result's visibility words: tuning launches overwrite them.
+  std::vector<std::pair<Result*, uint32_t*>> saved;
+  std::vector<CullScene> scenes;
+  std::vector<CullView> views;
+  uint32_t items = 0;
+  int rc = build_batch(c, jobs, n_jobs, 1, scenes, views, &items, nullptr, nullptr);
+  if (rc) return rc;
+  const std::string key = tune_key(scenes, views);
+  auto it = c->tune_cache.find(key);
+  if (it != c->tune_cache.end()) {
+    *out = it->second;
+    return DPCULL_OK;
+  }
+  for (size_t j = 0; j < n_jobs; ++j)
+    for (uint32_t v = 0; v < jobs[j].n_views; ++v) {
+      Result* r = get_result(c, jobs[j].results[v]);
+      uint32_t* copy = nullptr;
+      rc = dalloc(c, (void**)&copy, r->words_cap * 4);
+      if (rc) return rc;
+      cudaMemcpyAsync(copy, r->bits, r->words_cap * 4, cudaMemcpyDeviceToDevice, c->stream);
+      saved.push_back({r, copy});
+    }
+  dpcull_tuning best{(uint32_t)default_vpp(maxv), 1, 0, 0};
+  float best_ms = 1e30f;
+  const uint32_t vpps[4] = {1, 2, 4, 8};
+  for (uint32_t vpp : vpps) {
+    if (vpp > 1 && vpp / 2 >= maxv) continue;  // wider passes than any scene has views
+    std::vector<CullScene> sc;
+    std::vector<CullView> vw;
+    uint32_t it_items = 0;
+    rc = build_batch(c, jobs, n_jobs, vpp, sc, vw, &it_items, nullptr, nullptr);
+    if (rc || !it_items) break;
+    CullScene* ds = nullptr;
+    CullView* dv = nullptr;
+    if (dalloc(c, (void**)&ds, sc.size() * sizeof(CullScene)) || dalloc(c, (void**)&dv, vw.size() * sizeof(CullView))) {
+      rc = DPCULL_ERR_NO_MEMORY;
+      break;
+    }
+    cudaMemcpyAsync(ds, sc.data(), sc.size() * sizeof(CullScene), cudaMemcpyHostToDevice, c->stream);
+    cudaMemcpyAsync(dv, vw.data(), vw.size() * sizeof(CullView), cudaMemcpyHostToDevice, c->stream);
+    const int occ = cull_max_ctas_per_sm((int)vpp);
+    for (uint32_t tpt : {1u, 2u, 4u}) {
+      for (int cps = 1; cps <= occ; ++cps) {
+        dpcull_tuning t{vpp, tpt, (uint32_t)cps, 0};
+        float ms = 0;
+        rc = time_batch(c, ds, dv, (uint32_t)sc.size(), it_items, t, 3, &ms);
+        if (rc) break;
+        if (ms < best_ms) {
+          best_ms = ms;
+          best = t;
+        }
+      }
+      if (rc) break;
+    }
+    cudaStreamSynchronize(c->stream);
+    dfree(c, ds, sc.size() * sizeof(CullScene));
+    dfree(c, dv, vw.size() * sizeof(CullView));
+    if (rc) break;
+  }
+  for (auto& s : saved) {
+    cudaMemcpyAsync(s.first->bits, s.second, s.first->words_cap * 4, cudaMemcpyDeviceToDevice, c->stream);
+  }
+  cudaStreamSynchronize(c->stream);
+  for (auto& s : saved) dfree(c, s.second, s.first->words_cap * 4);
+  if (rc) return rc;
+  rc = check_device_errors(c);
+  if (rc) return rc;
+  c->tune_cache[key] = best;
+  tune_cache_store(key, best);
+  *out = best;
+  return DPCULL_OK;
+}
+
+int dpcull_plan_create(dpcull_ctx c, const dpcull_job* jobs, size_t n_jobs,
+                       const dpcull_tuning* tuning, dpcull_plan* out)
+{
+  if (!c || !out || (n_jobs && !jobs)) return fail(DPCULL_ERR_INVALID_ARGUMENT, "bad arguments");
+  dpcull_tuning t{};
+  if (tuning) {
+    t = *tuning;
+  } else {
+    int rc = dpcull_autotune(c, jobs, n_jobs, &t);
+    if (rc) return rc;
+  }
+  if (!valid_vpp(t.views_per_pass)) return fail(DPCULL_ERR_INVALID_ARGUMENT, "views_per_pass must be 1, 2, 4 or 8");
+  Plan p;
+  p.alive = true;
+  p.tuning = t;
+  int rc = build_batch(c, jobs, n_jobs, t.views_per_pass, p.scenes, p.views, &p.n_items, &p.groups, &p.results);
+  if (rc) return rc;
+  if (!p.n_items) return fail(DPCULL_ERR_STATE, "plan has no work (all groups empty)");
+  for (uint32_t g : p.groups) p.incarnations.push_back(c->groups[g].incarnation);
+  for (size_t j = 0; j < n_jobs; ++j) {
+    p.all_groups.push_back(jobs[j].group);
+    p.all_incarnations.push_back(c->groups[jobs[j].group].incarnation);
+  }
+  rc = dalloc(c, (void**)&p.d_scenes, p.scenes.size() * sizeof(CullScene));
+  if (!rc) rc = dalloc(c, (void**)&p.d_views, p.views.size() * sizeof(CullView));
+  if (rc) return rc;
+  CU(cudaMemcpyAsync(p.d_scenes, p.scenes.data(), p.scenes.size() * sizeof(CullScene), cudaMemcpyHostToDevice, c->stream));
+  for (int s = 0; s < 2; ++s) {
+    CU(cudaMallocHost((void**)&p.h_views[s], p.views.size() * sizeof(CullView)));
+    memcpy(p.h_views[s], p.views.data(), p.views.size() * sizeof(CullView));
+    CU(cudaEventCreateWithFlags(&p.done[s], cudaEventDisableTiming));
+    rc = plan_capture(c, p, s);
+    if (rc) return rc;
+  }
+  CU(cudaStreamSynchronize(c->stream));
+  c->plans.push_back(p);
+  *out = (dpcull_plan)(c->plans.size() - 1);
+  return DPCULL_OK;
+}
+
+int dpcull_plan_set_views(dpcull_ctx c, dpcull_plan ph, const float* vps)
+{
+  Plan* p = get_plan(c, ph);
+  if (!p || !vps) return fail(DPCULL_ERR_INVALID_ARGUMENT, "bad plan or matrices");
+  const int s = p->next;
+  if (p->pending[s]) {
+    CU(cudaEventSynchronize(p->done[s]));
+    p->pending[s] = false;
+  }
+  for (size_t v = 0; v < p->views.size(); ++v) {
+    memcpy(p->h_views[s][v].vp, vps + 16 * v, 64);
+    memcpy(p->views[v].vp, vps + 16 * v, 64);
+  }
+  p->fresh[s] = true;
+  return DPCULL_OK;
+}
+
+int dpcull_plan_launch(dpcull_ctx c, dpcull_plan ph)
+{
+  Plan* p = get_plan(c, ph);
+  if (!p) return fail(DPCULL_ERR_INVALID_ARGUMENT, "bad plan %u", ph);
+  for (size_t i = 0; i < p->all_groups.size(); ++i) {
+    Group* g = get_group(c, p->all_groups[i]);
+    if (!g || g->incarnation != p->all_incarnations[i])
+      return fail(DPCULL_ERR_STATE, "plan is stale: group %u changed since the plan was built", p->all_groups[i]);
+  }
+  for (size_t i = 0; i < p->groups.size(); ++i) {
+    Group* g = get_group(c, p->groups[i]);
+    if (g->soa != p->scenes[i].soa || g->mats != p->scenes[i].mats || g->n_mats != p->scenes[i].n_mats)
+      return fail(DPCULL_ERR_STATE, "plan is stale: group %u storage changed", p->groups[i]);
+    int rc = check_cull_ready(*g);
+    if (rc) return rc;
+  }
+  const int s = p->next;
+  if (!p->fresh[s]) {
+    if (p->pending[s]) {
+      CU(cudaEventSynchronize(p->done[s]));
+      p->pending[s] = false;
+    }
+    for (size_t v = 0; v < p->views.size(); ++v) memcpy(p->h_views[s][v].vp, p->views[v].vp, 64);
+  }
+  p->fresh[s] = false;
+  CU(cudaGraphLaunch(p->exec[s], c->stream));
+  CU(cudaEventRecord(p->done[s], c->stream));
+  p->pending[s] = true;
+  p->next ^= 1;
+  c->launches++;
+  return DPCULL_OK;
+}
+
+int dpcull_plan_tuning(dpcull_ctx c, dpcull_plan ph, dpcull_tuning* out)
+{
+  Plan* p = get_plan(c, ph);
+  if (!p || !out) return fail(DPCULL_ERR_INVALID_ARGUMENT, "bad plan %u", ph);
+  *out = p->tuning;
+  return DPCULL_OK;
+}
+
+int dpcull_plan_destroy(dpcull_ctx c, dpcull_plan ph)
+{
+  Plan* p = get_plan(c, ph);
+  if (!p) return fail(DPCULL_ERR_INVALID_ARGUMENT, "bad plan %u", ph);
+  cudaStreamSynchronize(c->stream);
+  for (int s = 0; s < 2; ++s) {
+    if (p->exec[s]) cudaGraphExecDestroy(p->exec[s]);
+    if (p->done[s]) cudaEventDestroy(p->done[s]);
+    if (p->h_views[s]) cudaFreeHost(p->h_views[s]);
+  }
+  dfree(c, p->d_scenes, p->scenes.size() * sizeof(CullScene));
+  dfree(c, p->d_views, p->views.size() * sizeof(CullView));
+  *p = Plan();
+  return DPCULL_OK;
+}
+
+// ---- transform tree ----------------------------------------------------------------
+int dpcull_tree_create(dpcull_ctx c, size_t capacity, dpcull_tree* out)
+{
+  if (!c || !out || !capacity || capacity > 0xFFFFFFFFull) return fail(DPCULL_ERR_INVALID_ARGUMENT, "bad arguments");
+  c->trees.emplace_back();
+  Tree& t = c->trees.back();
+  t.alive = true;
+  t.cap = capacity;
+  t.words = (capacity + 31) / 32;
+  int rc = dalloc(c, (void**)&t.local, capacity * 64);
+  if (!rc) rc = dalloc(c, (void**)&t.world, capacity * 64);
+  if (!rc) rc = dalloc(c, (void**)&t.dirty_local, t.words * 4);
+  if (!rc) rc = dalloc(c, (void**)&t.dirty_world, t.words * 4);
+  if (rc) return rc;
+  CU(cudaMemsetAsync(t.local, 0, capacity * 64, c->stream));
+  CU(cudaMemsetAsync(t.world, 0, capacity * 64, c->stream));
+  CU(cudaMemsetAsync(t.dirty_local, 0, t.words * 4, c->stream));
+  CU(cudaMemsetAsync(t.dirty_world, 0, t.words * 4, c->stream));
+  // Tree::Tree (Tree.cpp:38-47): the root (index 0) is the identity, local and world.
+  static const float I[16] = {1, 0, 0, 0, 0, 1, 0, 0, 0, 0, 1, 0, 0, 0, 0, 1};
+  CU(cudaMemcpyAsync(t.local, I, 64, cudaMemcpyHostToDevice, c->stream));
+  CU(cudaMemcpyAsync(t.world, I, 64, cudaMemcpyHostToDevice, c->stream));
+  CU(cudaStreamSynchronize(c->stream));
+  *out = (dpcull_tree)(c->trees.size() - 1);
+  return DPCULL_OK;
+}
+
+int dpcull_tree_destroy(dpcull_ctx c, dpcull_tree th)
+{
+  Tree* t = get_tree(c, th);
+  if (!t) return fail(DPCULL_ERR_INVALID_ARGUMENT, "bad tree %u", th);
+  cudaStreamSynchronize(c->stream);
+  dfree(c, t->local, t->cap * 64);
+  dfree(c, t->world, t->cap * 64);
+  dfree(c, t->dirty_local, t->words * 4);
+  dfree(c, t->dirty_world, t->words * 4);
+  dfree(c, t->entries, t->entries_cap * 8);
+  dfree(c, t->seg, t->seg_cap * 4);
+  *t = Tree();
+  return DPCULL_OK;
+}
+
+int dpcull_tree_resize(dpcull_ctx c, dpcull_tree th, size_t capacity)
+{
+  Tree* t = get_tree(c, th);
+  if (!t) return fail(DPCULL_ERR_INVALID_ARGUMENT, "bad tree %u", th);
+  if (capacity < t->cap || capacity > 0xFFFFFFFFull) return fail(DPCULL_ERR_INVALID_ARGUMENT, "capacity can only grow");
+  if (capacity == t->cap) return DPCULL_OK;
+  const size_t words = (capacity + 31) / 32;
+  float *local = nullptr, *world = nullptr;
+  uint32_t *dl = nullptr, *dw = nullptr;
+  int rc = dalloc(c, (void**)&local, capacity * 64);
+  if (!rc) rc = dalloc(c, (void**)&world, capacity * 64);
+  if (!rc) rc = dalloc(c, (void**)&dl, words * 4);
+  if (!rc) rc = dalloc(c, (void**)&dw, words * 4);
+  if (rc) {
+    dfree(c, local, capacity * 64);
+    dfree(c, world, capacity * 64);
+    dfree(c, dl, words * 4);
+    return rc;
+  }
+  CU(cudaMemsetAsync(local, 0, capacity * 64, c->stream));
+  CU(cudaMemsetAsync(world, 0, capacity * 64, c->stream));
+  CU(cudaMemsetAsync(dl, 0, words * 4, c->stream));
+  CU(cudaMemsetAsync(dw, 0, words * 4, c->stream));
+  CU(cudaMemcpyAsync(local, t->local, t->cap * 64, cudaMemcpyDeviceToDevice, c->stream));
+  CU(cudaMemcpyAsync(world, t->world, t->cap * 64, cudaMemcpyDeviceToDevice, c->stream));
+  CU(cudaMemcpyAsync(dl, t->dirty_local, t->words * 4, cudaMemcpyDeviceToDevice, c->stream));
+  CU(cudaMemcpyAsync(dw, t->dirty_world, t->words * 4, cudaMemcpyDeviceToDevice, c->stream));
+  CU(cudaStreamSynchronize(c->stream));
+  dfree(c, t->local, t->cap * 64);
+  dfree(c, t->world, t->cap * 64);
+  dfree(c, t->dirty_local, t->words * 4);
+  dfree(c, t->dirty_world, t->words * 4);
+  t->local = local;
+  t->world = world;
+  t->dirty_local = dl;
+  t->dirty_world = dw;
+  t->cap = capacity;
+  t->words = words;
+  return DPCULL_OK;
+}
+
+int dpcull_tree_set_structure(dpcull_ctx c, dpcull_tree th, size_t n_entries, const uint32_t* pairs,
+                              size_t n_levels, const uint32_t* level_offsets)
+{
+  Tree* t = get_tree(c, th);
+  if (!t) return fail(DPCULL_ERR_INVALID_ARGUMENT, "bad tree %u", th);
+  if (n_entries && (!pairs || !level_offsets)) return fail(DPCULL_ERR_INVALID_ARGUMENT, "null arrays");
+  if (n_levels && level_offsets[n_levels] != n_entries)
+    return fail(DPCULL_ERR_INVALID_ARGUMENT, "level offsets do not cover the entries");
+  for (size_t i = 0; i < 2 * n_entries; ++i)
+    if (pairs[i] >= t->cap) return fail(DPCULL_ERR_OUT_OF_RANGE, "transform %u >= capacity %zu", pairs[i], t->cap);
+  // Split each level into segments in which no entry reads a world matrix (or its dirty
+  // bit) that another entry of the same segment writes.  The reference reads them in
+  // list order, so a reader that follows its writer starts a new segment and a reader
+  // that precedes it ends the segment before the writer.
+  std::vector<uint32_t> seg;
+  std::vector<uint8_t> written(t->cap, 0), read(t->cap, 0);
+  std::vector<uint32_t> touched;
+  for (size_t l = 0; l < n_levels; ++l) {
+    const uint32_t b = level_offsets[l], e = level_offsets[l + 1];
+    if (b > e || e > n_entries) return fail(DPCULL_ERR_INVALID_ARGUMENT, "bad level offsets");
+    if (b == e) continue;
+    seg.push_back(b);
+    for (uint32_t i = b; i < e; ++i) {
+      const uint32_t p = pairs[2 * i], x = pairs[2 * i + 1];
+      if (written[p] || read[x] || written[x]) {
+        seg.push_back(i);
+        for (uint32_t k : touched) written[k] = read[k] = 0;
+        touched.clear();
+      }
+      written[x] = 1;
+      read[p] = 1;
+      touched.push_back(x);
+      touched.push_back(p);
+    }
+    for (uint32_t k : touched) written[k] = read[k] = 0;
+    touched.clear();
+  }
+  seg.push_back((uint32_t)n_entries);
+  // Launch schedule: runs of narrow segments share one single-CTA launch.
+  const uint32_t kNarrow = 4096;
+  t->schedule.clear();
+  const size_t nseg = seg.size() - 1;
+  size_t s = 0;
+  while (s < nseg) {
+    if (seg[s + 1] - seg[s] <= kNarrow) {
+      size_t e = s;
+      while (e < nseg && seg[e + 1] - seg[e] <= kNarrow) ++e;
+      t->schedule.push_back({true, (uint32_t)s, (uint32_t)e});
+      s = e;
+    } else {
+      t->schedule.push_back({false, seg[s], seg[s + 1]});
+      ++s;
+    }
+  }
+  if (n_entries > t->entries_cap) {
+    dfree(c, t->entries, t->entries_cap * 8);
+    t->entries = nullptr;
+    int rc = dalloc(c, (void**)&t->entries, n_entries * 8);
+    if (rc) return rc;
+    t->entries_cap = n_entries;
+  }
+  if (seg.size() > t->seg_cap) {
+    dfree(c, t->seg, t->seg_cap * 4);
+    t->seg = nullptr;
+    int rc = dalloc(c, (void**)&t->seg, seg.size() * 4);
+    if (rc) return rc;
+    t->seg_cap = seg.size();
+  }
+  if (n_entries) CU(cudaMemcpyAsync(t->entries, pairs, n_entries * 8, cudaMemcpyHostToDevice, c->stream));
+  CU(cudaMemcpyAsync(t->seg, seg.data(), seg.size() * 4, cudaMemcpyHostToDevice, c->stream));
+  CU(cudaStreamSynchronize(c->stream));
+  return DPCULL_OK;
+}
+
+static int tree_scatter(dpcull_ctx c, Tree* t, float* dst, size_t k, const uint32_t* index,
+                        const float* matrices, uint32_t* dirty)
+{
+  for (size_t i = 0; i < k; ++i)
+    if (index[i] >= t->cap) return fail(DPCULL_ERR_OUT_OF_RANGE, "transform %u >= capacity %zu", index[i], t->cap);
+  float* d = nullptr;
+  uint32_t* di = nullptr;
+  int rc = dalloc(c, (void**)&d, 64 * k);
+  if (rc) return rc;
+  rc = dalloc(c, (void**)&di, 4 * k);
+  if (rc) {
+    dfree(c, d, 64 * k);
+    return rc;
+  }
+  cudaMemcpyAsync(d, matrices, 64 * k, cudaMemcpyHostToDevice, c->stream);
+  cudaMemcpyAsync(di, index, 4 * k, cudaMemcpyHostToDevice, c->stream);
+  launch_scatter_matrices(dst, d, di, (uint32_t)k, dirty, c->stream);
+  c->launches++;
+  cudaError_t e = cudaStreamSynchronize(c->stream);
+  dfree(c, d, 64 * k);
+  dfree(c, di, 4 * k);
+  if (e != cudaSuccess) return cuda_fail(e, "tree scatter");
+  return DPCULL_OK;
+}
+
+int dpcull_tree_set_locals(dpcull_ctx c, dpcull_tree th, size_t k, const uint32_t* index, const float* m)
+{
+  Tree* t = get_tree(c, th);
+  if (!t) return fail(DPCULL_ERR_INVALID_ARGUMENT, "bad tree %u", th);
+  if (!k) return DPCULL_OK;
+  if (!index || !m) return fail(DPCULL_ERR_INVALID_ARGUMENT, "null arrays");
+  return tree_scatter(c, t, t->local, k, index, m, t->dirty_local);
+}
+
+int dpcull_tree_set_worlds(dpcull_ctx c, dpcull_tree th, size_t k, const uint32_t* index, const float* m)
+{
+  Tree* t = get_tree(c, th);
+  if (!t) return fail(DPCULL_ERR_INVALID_ARGUMENT, "bad tree %u", th);
+  if (!k) return DPCULL_OK;
+  if (!index || !m) return fail(DPCULL_ERR_INVALID_ARGUMENT, "null arrays");
+  return tree_scatter(c, t, t->world, k, index, m, nullptr);
+}
+
+int dpcull_tree_compute(dpcull_ctx c, dpcull_tree th)
+{
+  Tree* t = get_tree(c, th);
+  if (!t) return fail(DPCULL_ERR_INVALID_ARGUMENT, "bad tree %u", th);
+  CU(cudaMemsetAsync(t->dirty_world, 0, t->words * 4, c->stream));
+  XformLaunch a{t->entries, t->seg, t->local, t->world, t->dirty_local, t->dirty_world};
+  for (const TreeLaunch& L : t->schedule) {
+    int rc = L.single_cta ? launch_xform_cta(a, L.a, L.b, c->stream)
+                          : launch_xform_range(a, L.a, L.b, c->stream);
+    if (rc) return cuda_fail(cudaGetLastError(), "tree launch");
+    c->launches++;
+  }
+  CU(cudaMemsetAsync(t->dirty_local, 0, t->words * 4, c->stream));
+  return DPCULL_OK;
+}
+
+int dpcull_tree_world_device(dpcull_ctx c, dpcull_tree th, const float** world, size_t* count)
+{
+  Tree* t = get_tree(c, th);
+  if (!t || !world || !count) return fail(DPCULL_ERR_INVALID_ARGUMENT, "bad arguments");
+  *world = t->world;
+  *count = t->cap;
+  return DPCULL_OK;
+}
+
+int dpcull_tree_world(dpcull_ctx c, dpcull_tree th, size_t first, size_t count, float* out)
+{
+  Tree* t = get_tree(c, th);
+  if (!t || (count && !out)) return fail(DPCULL_ERR_INVALID_ARGUMENT, "bad arguments");
+  if (first + count > t->cap) return fail(DPCULL_ERR_OUT_OF_RANGE, "range past capacity");
+  if (count) CU(cudaMemcpyAsync(out, t->world + 16 * first, count * 64, cudaMemcpyDeviceToHost, c->stream));
+  CU(cudaStreamSynchronize(c->stream));
+  return DPCULL_OK;
+}
+
+int dpcull_tree_dirty_world(dpcull_ctx c, dpcull_tree th, uint32_t* words, size_t n_words)
+{
+  Tree* t = get_tree(c, th);
+  if (!t || !words) return fail(DPCULL_ERR_INVALID_ARGUMENT, "bad arguments");
+  const size_t k = std::min(n_words, t->words);
+  CU(cudaMemcpyAsync(words, t->dirty_world, k * 4, cudaMemcpyDeviceToHost, c->stream));
+  CU(cudaStreamSynchronize(c->stream));
+  return DPCULL_OK;
+}
+
+}  // extern "C"

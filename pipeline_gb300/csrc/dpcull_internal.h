@@ -1,0 +1,109 @@
+// dpcull_internal.h -- shared host/device definitions of the GB300 culling backend.
+//
+// Data layout in HBM (one allocation per culling group):
+//   lower.x | lower.y | lower.z | extent.x | extent.y | extent.z   float[cap] each
+//   transform index                                                  uint32[cap]
+// cap is the object count rounded up to a whole tile (kTileObjects), so every 128-bit
+// load of a tile stays inside the allocation.  World matrices are Mat44f rows
+// (4 x float4, row-major, row-vector convention) gathered by transform index.
+// A result (one group x one view) owns its visibility bit array (bit i of word i/32 is
+// object i, the ResultBitSet layout), its changed-object list and its look-back status
+// words (one per tile).
+#pragma once
+
+#include <cstddef>
+#include <cstdint>
+
+namespace dpcull {
+
+constexpr int kThreads = 256;                      // threads per CTA
+constexpr int kObjPerThread = 4;                   // one float4 of each SoA row
+constexpr int kTileObjects = kThreads * kObjPerThread;  // 1024 objects per tile
+constexpr int kTileWords = kTileObjects / 32;      // 32 bit-array words per tile and view
+constexpr int kMaxViewsPerPass = 8;                // views evaluated per object load
+constexpr uint32_t kMaxObjects = (1u << 30) - 1;   // changed counts are packed in 30 bits
+
+// Look-back status word: epoch (32) | flag (2) | value (30).
+constexpr uint32_t kFlagAggregate = 1;
+constexpr uint32_t kFlagPrefix = 2;
+
+// Error bits reported through CullControl::error.
+constexpr uint32_t kErrBadTransform = 1u;   // transform index >= matrix count
+constexpr uint32_t kErrLookbackTimeout = 2u; // bounded wait for a predecessor tile expired
+
+struct CullScene {
+  const float* soa;        // base of the group's SoA block
+  const float* mats;       // [n_mats][16]
+  uint32_t cap;            // SoA row stride (objects)
+  uint32_t n_objects;
+  uint32_t n_mats;
+  uint32_t view_begin;     // first CullView of this scene
+  uint32_t n_views;
+  uint32_t n_vgroups;      // ceil(n_views / views per pass)
+  uint32_t n_tiles;
+  uint32_t item_begin;     // first work item of this scene (items = tiles x view groups)
+};
+
+struct CullView {
+  float vp[16];
+  uint32_t* bits;                 // previous visibility on entry, new visibility on exit
+  uint32_t* changed;              // ascending changed-object list
+  uint32_t* n_changed;            // total, written by the scene's last tile
+  unsigned long long* status;     // one look-back word per tile
+};
+
+struct CullControl {
+  unsigned int ticket;     // next work item
+  unsigned int done;       // CTAs finished
+  unsigned int epoch;      // current launch's epoch (advanced by the last CTA)
+  unsigned int stride;     // epoch increment (distinct per control block)
+  unsigned int error;      // sticky kErr* bits
+  unsigned int error_info; // first offending index
+  unsigned int pad[2];
+};
+
+struct CullLaunch {
+  const CullScene* scenes;   // device array, or nullptr to use `one_scene`
+  const CullView* views;     // device array, or nullptr to use `one_view`
+  uint32_t n_scenes;
+  uint32_t n_items;
+  uint32_t items_per_ticket; // tiles claimed per ticket ("tiles per CTA" tuning knob)
+  uint32_t spin_limit;       // look-back wait budget (polls)
+  CullControl* ctl;
+  CullScene one_scene;
+  CullView one_view;
+};
+
+// Launchers (cull.cu).  vpp = views per pass (1, 2, 4 or 8).
+int launch_cull(const CullLaunch& args, int grid, int vpp, void* stream);
+int cull_max_ctas_per_sm(int vpp);
+
+// Transform propagation (xform.cu).
+struct XformLaunch {
+  const uint2* entries;      // (parent, transform) in level order
+  const uint32_t* seg;       // segment offsets into entries
+  const float* local;        // [cap][16]
+  float* world;              // [cap][16]
+  const uint32_t* dirty_local;
+  uint32_t* dirty_world;
+};
+// Segments [s0, s1) inside one CTA (narrow levels), or entries [begin, end) of one wide
+// segment over a grid.
+int launch_xform_cta(const XformLaunch& a, uint32_t s0, uint32_t s1, void* stream);
+int launch_xform_range(const XformLaunch& a, uint32_t begin, uint32_t end, void* stream);
+int launch_scatter_matrices(float* dst, const float* src, const uint32_t* idx, uint32_t k,
+                            uint32_t* dirty_bits, void* stream);
+int launch_scatter_objects(float* soa, uint32_t cap, const float* src, const uint32_t* idx,
+                           uint32_t k, void* stream);
+
+// Bounding box (bbox.cu): partials has room for bbox_partials_needed() floats.
+size_t bbox_partials_needed(uint32_t n_objects);
+int launch_bbox(const float* soa, uint32_t cap, uint32_t n, const float* mats, float* partials,
+                unsigned int* counter, float* out8, void* stream);
+
+// Result remap on object removal (api helpers in cull.cu).
+int launch_move_bit(uint32_t* bits, uint32_t size_bits, uint32_t old_index, uint32_t new_index,
+                    void* stream);
+int launch_move_object(float* soa, uint32_t cap, uint32_t from, uint32_t to, void* stream);
+
+}  // namespace dpcull

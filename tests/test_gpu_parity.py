@@ -1,0 +1,343 @@
+"""CUDA backend against the reference: golden fixtures written by the reference itself and
+the oracle port on the same seeded inputs.  Every comparison is bit-exact (visibility
+words, changed lists, world matrices, bounding boxes).  All calls go through the C ABI."""
+import numpy as np
+import pytest
+
+import oracle
+from conftest import f32_bits, golden_scene_names, load_golden
+from pipeline_gb300 import native
+from pipeline_gb300 import workloads as W
+
+pytestmark = pytest.mark.gpu
+
+
+def unpack(bits, n):
+    return np.unpackbits(np.ascontiguousarray(bits, np.uint32).view(np.uint8), bitorder="little")[:n]
+
+
+def extent_of(lower, upper):
+    """What objectSetBoundingBox stores: Box3f(lower, upper) then upper - lower in FP32."""
+    lo = np.minimum(lower, upper)  # Box3f's constructor orders the corners (non-NaN inputs)
+    hi = np.maximum(lower, upper)
+    nan = np.isnan(lower) | np.isnan(upper)
+    lo = np.where(nan, np.float32(0), lo)
+    return lo.astype(np.float32), (hi - lo).astype(np.float32)
+
+
+def box3_lower_extent(lower, upper):
+    """Exact Box3f(lower, upper) -> (lower, size) semantics per component, NaN included."""
+    FMAX = np.float32(np.finfo(np.float32).max)
+    lo = np.full(lower.shape, FMAX, np.float32)
+    hi = np.full(lower.shape, -FMAX, np.float32)
+    for p in (lower, upper):
+        m = lo > p
+        lo = np.where(m, p, lo)
+        m = hi < p
+        hi = np.where(m, p, hi)
+    return lo.astype(np.float32), (hi - lo).astype(np.float32)
+
+
+def setup_group(ctx, lower, upper, xform, mats):
+    lo, ex = box3_lower_extent(np.asarray(lower, np.float32), np.asarray(upper, np.float32))
+    g = ctx.group_create()
+    ctx.group_set_objects(g, lo, ex, xform)
+    ctx.group_set_matrices(g, mats)
+    return g
+
+
+@pytest.mark.parametrize("name", golden_scene_names())
+def test_golden_scene(ctx, name):
+    z = load_golden(name)
+    n = len(z["xform"])
+    g = setup_group(ctx, z["lower"], z["upper"], z["xform"], z["mats"])
+    r = ctx.result_create(g)
+    order = list(range(n))  # group index -> object id
+    for k, vp in enumerate(z["vps"]):
+        ctx.cull(g, r, vp)
+        ch = ctx.result_changed(r)
+        assert np.array_equal(np.asarray(order)[ch], z[f"changed{k}"]), (name, k)
+        assert np.array_equal(ctx.result_bits(r), z[f"bits{k}"]), (name, k)
+    lo, hi = ctx.group_bounding_box(g)
+    assert np.array_equal(f32_bits(np.concatenate([lo, hi])), f32_bits(z["bbox"])), name
+    for o in z["removals"]:
+        hole = order.index(int(o))
+        ctx.group_remove_object(g, hole)
+        order[hole] = order[-1]
+        order.pop()
+    if len(z["removals"]) or len(z["dirty"]):
+        ctx.cull(g, r, z["vps"][0])
+        assert np.array_equal(np.asarray(order, np.int32), z["order_after"])
+        ch = ctx.result_changed(r)
+        assert np.array_equal(np.asarray(order)[ch], z["changed_after"]), name
+        assert np.array_equal(ctx.result_bits(r), z["bits_after"]), name
+    ctx.group_destroy(g)
+
+
+def test_golden_tree(ctx):
+    from pipeline_gb300.transform import Tree
+
+    z = load_golden("tree_small.npz")
+    pairs, locs = z["pairs"], z["locals"]
+    used = locs.shape[0]
+    words = (used + 31) // 32
+    t = Tree(ctx)
+    for p, x in pairs:
+        assert t.add_transform(int(p), locs[x]) == x
+    t.compute()
+    assert np.array_equal(f32_bits(t.world_matrices(used)), f32_bits(z["world0"]))
+    assert np.array_equal(t.dirty_world_matrices()[:words], z["dirty0"])
+    for k, i in enumerate(z["upd"]):
+        t.update_local_matrix(int(i), z["upd_locals"][k])
+    t.compute()
+    assert np.array_equal(f32_bits(t.world_matrices(used)), f32_bits(z["world1"]))
+    assert np.array_equal(t.dirty_world_matrices()[:words], z["dirty1"])
+    victim = int(z["victim"])
+    new_parent = int(pairs[z["level_offsets"][2]][1])
+    t.remove_transform(victim)
+    assert t.add_transform(new_parent, locs[victim]) == victim
+    for i in range(1, used):
+        t.update_local_matrix(i, locs[i])
+    t.compute()
+    assert np.array_equal(f32_bits(t.world_matrices(used)), f32_bits(z["world2"]))
+    assert np.array_equal(t.dirty_world_matrices()[:words], z["dirty2"])
+
+
+def port_frames(sc, vps):
+    """Bits and changed lists of consecutive culls, from the oracle port."""
+    n = len(sc["xform"])
+    obbs = oracle.build_obbs(sc["lower"], sc["extent"], sc["xform"], sc["mats"])
+    prev = np.full((n + 31) // 32, 0xFFFFFFFF, np.uint32)
+    if n % 32:
+        prev[-1] = (1 << (n % 32)) - 1
+    out = []
+    for vp in vps:
+        bits = oracle.cull_obbs(obbs, vp, threads=8)
+        ch = oracle.update_changed(prev, bits, n)
+        out.append((bits, ch))
+    return out
+
+
+def test_plain_config_full_size(ctx):
+    """100k objects, own matrices, two frames with a 1 degree yaw (the plain configuration)."""
+    sc = W.plain_scene(0, 100_000)
+    g = setup_group(ctx, sc["lower"], sc["upper"], sc["xform"], sc["mats"])
+    r = ctx.result_create(g)
+    exp = port_frames(sc, sc["vps"])
+    for vp, (bits, ch) in zip(sc["vps"], exp):
+        ctx.cull(g, r, vp)
+        assert np.array_equal(ctx.result_bits(r), bits)
+        assert np.array_equal(ctx.result_changed(r), ch)
+    assert len(exp[1][1]) > 0  # the yaw changes some objects
+    ctx.group_destroy(g)
+
+
+@pytest.mark.parametrize("n", [0, 1, 31, 32, 33, 1023, 1024, 1025, 4097, 70001])
+def test_ragged_sizes(ctx, n):
+    rng = np.random.default_rng(n)
+    lower, upper, extent = W.random_boxes(rng, n)
+    mats = W.random_matrices(rng, max(n // 3, 1))
+    mats[:, 12:15] *= np.float32(0.02)
+    xform = rng.integers(0, mats.shape[0], n, dtype=np.uint32)
+    sc = dict(lower=lower, extent=extent, xform=xform, mats=mats)
+    vps = W.f32(W.cube_face_views()[:3])
+    g = setup_group(ctx, lower, upper, xform, mats)
+    r = ctx.result_create(g)
+    for vp, (bits, ch) in zip(vps, port_frames(sc, vps)):
+        ctx.cull(g, r, vp)
+        assert np.array_equal(ctx.result_bits(r), bits[: (n + 31) // 32])
+        assert np.array_equal(ctx.result_changed(r), ch)
+    ctx.group_destroy(g)
+
+
+def test_batched_equals_plain_and_port(ctx):
+    """Uneven scenes x 1-6 views in one persistent launch == per-view plain launches == port."""
+    scenes = W.batched_scenes(seed=7, n_scenes=10, nmin=500, nmax=60_000)
+    jobs, plain, exp = [], [], []
+    for s in scenes:
+        g = setup_group(ctx, s["lower"], s["upper"], s["xform"], s["mats"])
+        rs = [ctx.result_create(g) for _ in s["vps"]]
+        jobs.append((g, rs, s["vps"]))
+        rp = [ctx.result_create(g) for _ in s["vps"]]
+        plain.append((g, rp, s["vps"]))
+        exp.append([port_frames(s, [vp])[0] for vp in s["vps"]])
+    for tuning in (None, dict(views_per_pass=1, tiles_per_ticket=1, ctas_per_sm=1),
+                   dict(views_per_pass=2, tiles_per_ticket=4, ctas_per_sm=2),
+                   dict(views_per_pass=8, tiles_per_ticket=2, ctas_per_sm=0)):
+        # fresh results each round: reset by culling through new results
+        jobs_t = [(g, [ctx.result_create(g) for _ in vps], vps) for g, _, vps in jobs]
+        ctx.cull_batched(jobs_t, tuning)
+        for (g, rs, vps), e in zip(jobs_t, exp):
+            for r, (bits, ch) in zip(rs, e):
+                assert np.array_equal(ctx.result_bits(r), bits), tuning
+                assert np.array_equal(ctx.result_changed(r), ch), tuning
+    for (g, rp, vps), e in zip(plain, exp):
+        for r, vp, (bits, ch) in zip(rp, vps, e):
+            ctx.cull(g, r, vp)
+            assert np.array_equal(ctx.result_bits(r), bits)
+            assert np.array_equal(ctx.result_changed(r), ch)
+    for g, _, _ in jobs:
+        ctx.group_destroy(g)
+
+
+def test_plan_graph_frames(ctx):
+    """A captured plan replayed over several camera frames (double-buffered view upload)."""
+    sc = W.stress_scene(seed=9, n_objects=300_000, n_transforms=20_000)
+    g = setup_group(ctx, sc["lower"], sc["upper"], sc["xform"], sc["mats"])
+    rs = [ctx.result_create(g) for _ in range(8)]
+    p = ctx.plan_create([(g, rs, sc["vps"])], dict(views_per_pass=4, tiles_per_ticket=2, ctas_per_sm=0))
+    rng = np.random.default_rng(3)
+    frames = [sc["vps"]] + [np.stack([W.jitter_view(rng, v) for v in sc["vps"]]) for _ in range(4)]
+    obbs = oracle.build_obbs(sc["lower"], sc["extent"], sc["xform"], sc["mats"])
+    n = 300_000
+    prev = [np.full((n + 31) // 32, 0xFFFFFFFF, np.uint32) for _ in range(8)]
+    for vps in frames:
+        ctx.plan_set_views(p, vps)
+        ctx.plan_launch(p)
+        for v in range(8):
+            bits = oracle.cull_obbs(obbs, vps[v], threads=8)
+            ch = oracle.update_changed(prev[v], bits, n)
+            assert np.array_equal(ctx.result_bits(rs[v]), bits)
+            assert np.array_equal(ctx.result_changed(rs[v]), ch)
+    # a plan without set_views replays its last matrices
+    ctx.plan_launch(p)
+    for v in range(8):
+        assert len(ctx.result_changed(rs[v])) == 0
+    ctx.plan_destroy(p)
+    ctx.group_destroy(g)
+
+
+def test_plan_autotuned(ctx, tmp_path, monkeypatch):
+    sc = W.stress_scene(seed=10, n_objects=200_000, n_transforms=5000)
+    g = setup_group(ctx, sc["lower"], sc["upper"], sc["xform"], sc["mats"])
+    rs = [ctx.result_create(g) for _ in range(8)]
+    p = ctx.plan_create([(g, rs, sc["vps"])])
+    t = ctx.plan_tuning(p)
+    assert t["views_per_pass"] in (1, 2, 4, 8)
+    ctx.plan_launch(p)
+    obbs = oracle.build_obbs(sc["lower"], sc["extent"], sc["xform"], sc["mats"])
+    for v in range(8):
+        assert np.array_equal(ctx.result_bits(rs[v]), oracle.cull_obbs(obbs, sc["vps"][v], 8))
+    ctx.plan_destroy(p)
+    ctx.group_destroy(g)
+
+
+def test_hierarchy_propagate_then_cull(ctx):
+    """Tree propagation on the GPU feeding the cull through device-bound world matrices."""
+    from pipeline_gb300.transform import Tree
+
+    sc = W.hierarchy_scene(seed=4, n_objects=400_000, frames=3)
+    t = Tree(ctx)
+    for p, x in sc["pairs"]:
+        t.add_transform(int(p), sc["locals"][x])
+    t.compute()
+    used = sc["n_transforms"]
+    # oracle: the same propagation on arrays
+    world = np.zeros((used, 16), np.float32)
+    world[0] = np.eye(4, dtype=np.float32).reshape(16)
+    dl = np.zeros((used + 31) // 32 + 1, np.uint32)
+    dl[:] = 0xFFFFFFFF
+    dw = np.zeros_like(dl)
+    oracle.propagate(sc["pairs"], sc["locals"], world, dl, dw)
+    assert np.array_equal(f32_bits(t.world_matrices(used)), f32_bits(world))
+    dev, count = t.world_device()
+    g = ctx.group_create()
+    lo, ex = box3_lower_extent(sc["lower"], sc["upper"])
+    ctx.group_set_objects(g, lo, ex, sc["xform"])
+    ctx.group_bind_device_matrices(g, dev, count)
+    r = ctx.result_create(g)
+    s = dict(lower=lo, extent=ex, xform=sc["xform"], mats=world)
+    for vp, (bits, ch) in zip(sc["vps"], port_frames(s, sc["vps"])):
+        ctx.cull(g, r, vp)
+        assert np.array_equal(ctx.result_bits(r), bits)
+        assert np.array_equal(ctx.result_changed(r), ch)
+    ctx.group_destroy(g)
+
+
+def test_stress_full_size_eight_views(ctx):
+    """16M objects over 1M shared transforms, 8 views, one batched launch: every visibility
+    word of every view equals the oracle's (multi-threaded port)."""
+    sc = W.stress_scene()
+    n = len(sc["xform"])
+    g = setup_group(ctx, sc["lower"], sc["upper"], sc["xform"], sc["mats"])
+    rs = [ctx.result_create(g) for _ in range(8)]
+    ctx.cull_batched([(g, rs, sc["vps"])])
+    obbs = oracle.build_obbs(sc["lower"], sc["extent"], sc["xform"], sc["mats"])
+    for v in range(8):
+        bits = oracle.cull_obbs(obbs, sc["vps"][v], threads=16)
+        assert np.array_equal(ctx.result_bits(rs[v]), bits), v
+        ch = ctx.result_changed(rs[v])
+        # first cull: changed = invisible objects, ascending
+        vis = unpack(bits, n)
+        assert np.array_equal(ch, np.flatnonzero(vis == 0))
+    del obbs
+    ctx.group_destroy(g)
+
+
+def test_bad_transform_index_is_an_error(ctx):
+    rng = np.random.default_rng(1)
+    lower, upper, extent = W.random_boxes(rng, 100)
+    xform = np.arange(100, dtype=np.uint32)
+    g = ctx.group_create()
+    ctx.group_set_objects(g, lower, extent, xform)
+    ctx.group_set_matrices(g, W.random_matrices(rng, 50))
+    r = ctx.result_create(g)
+    with pytest.raises(native.DpcullError) as e:
+        ctx.cull(g, r, W.f32([W.perspective()])[0])
+    assert e.value.code == native.ERR_OUT_OF_RANGE
+    g2 = ctx.group_create()
+    with pytest.raises(native.DpcullError):
+        ctx.cull(g2, r, W.f32([W.perspective()])[0])  # result of another group
+    ctx.group_destroy(g)
+    ctx.group_destroy(g2)
+
+
+def test_object_updates_and_appends(ctx):
+    rng = np.random.default_rng(2)
+    n = 5000
+    lower, upper, extent = W.random_boxes(rng, n)
+    mats = W.random_matrices(rng, 100)
+    mats[:, 12:15] *= np.float32(0.01)
+    xform = rng.integers(0, 100, n, dtype=np.uint32)
+    g = ctx.group_create()
+    ctx.group_set_objects(g, lower, extent, xform)
+    ctx.group_set_matrices(g, mats)
+    r = ctx.result_create(g)
+    vp = W.f32(W.cube_face_views())[4]
+    ctx.cull(g, r, vp)
+    # move some objects, append some, update some matrices in place
+    idx = rng.choice(n, 300, replace=False).astype(np.uint32)
+    l2, u2, e2 = W.random_boxes(rng, 300)
+    x2 = rng.integers(0, 100, 300, dtype=np.uint32)
+    ctx.group_update_objects(g, idx, l2, e2, x2)
+    lower[:, idx], extent[:, idx], xform[idx] = l2, e2, x2
+    l3, u3, e3 = W.random_boxes(rng, 77)
+    x3 = rng.integers(0, 100, 77, dtype=np.uint32)
+    ctx.group_append_objects(g, l3, e3, x3)
+    lower, extent, xform = np.c_[lower, l3], np.c_[extent, e3], np.r_[xform, x3]
+    mi = np.array([3, 50, 99], np.uint32)
+    mats[mi] = W.random_matrices(rng, 3)
+    ctx.group_update_matrices(g, mi, mats)
+    prev = ctx.result_bits(r).copy()
+    ctx.cull(g, r, vp)
+    bits = oracle.cull_bits(lower, extent, xform, mats, vp)
+    assert np.array_equal(ctx.result_bits(r), bits)
+    # appended objects start visible (ResultBitSet resize), others compare with prev
+    m = n + 77
+    pv = np.zeros((m + 31) // 32, np.uint32)
+    pv[: prev.shape[0]] = prev
+    for i in range(n, m):
+        pv[i // 32] |= np.uint32(1 << (i % 32))
+    assert np.array_equal(ctx.result_changed(r), oracle.changed_list(pv, bits, m))
+    ctx.group_destroy(g)
+
+
+def test_kernel_launch_counter(ctx):
+    sc = W.plain_scene(5, 5000)
+    g = setup_group(ctx, sc["lower"], sc["upper"], sc["xform"], sc["mats"])
+    r = ctx.result_create(g)
+    before = ctx.kernel_launches
+    ctx.cull(g, r, sc["vps"][0])
+    ctx.synchronize()
+    assert ctx.kernel_launches > before
+    ctx.group_destroy(g)
