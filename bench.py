@@ -163,6 +163,16 @@ class Stress:
                 + 4 * changed_total)
 
 
+def parse_tuning(s: str | None) -> dict | None:
+    """JSON, or 'views_per_pass,tiles_per_ticket,ctas_per_sm'; None = run the autotuner."""
+    if not s:
+        return None
+    if s.strip().startswith("{"):
+        return json.loads(s)
+    a, b, c = (int(x) for x in s.split(","))
+    return {"views_per_pass": a, "tiles_per_ticket": b, "ctas_per_sm": c}
+
+
 # ---- our arm ---------------------------------------------------------------------------------
 def run_ours(args, dist: Dist) -> dict | None:
     import torch
@@ -174,9 +184,9 @@ def run_ours(args, dist: Dist) -> dict | None:
     dist.barrier()
     device = dist.local
     torch.cuda.set_device(device)
-    wl = Stress(seed=3 + 1000 * dist.rank)
+    wl = Stress(seed=3 + 1000 * dist.rank, n=args.objects, t=args.transforms)
     ctx = native.Context(device)
-    wl.setup(ctx, json.loads(args.tuning) if args.tuning else None)
+    wl.setup(ctx, parse_tuning(args.tuning))
     tuning = ctx.plan_tuning(wl.plan)
     rng = np.random.default_rng(17 + dist.rank)
     frames = make_frames(rng, wl.sc["vps"], args.warmup + args.steps + 1)
@@ -379,12 +389,14 @@ def run_reference(args, dist: Dist) -> dict | None:
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=50)
+    ap.add_argument("--steps", type=int, default=400)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="stress", choices=["stress"])
     ap.add_argument("--tuning", default=None, help="JSON tuning (default: autotuner)")
     ap.add_argument("--cpu-sample", type=int, default=1_000_000)
+    ap.add_argument("--objects", type=int, default=STRESS_N, help="objects per GPU (smaller cases for profiling)")
+    ap.add_argument("--transforms", type=int, default=STRESS_T)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)

@@ -69,6 +69,11 @@ void* dpcull_ctx_stream(dpcull_ctx ctx);
 uint64_t dpcull_ctx_kernel_launches(dpcull_ctx ctx);
 /* Device bytes currently held by the context. */
 uint64_t dpcull_ctx_device_bytes(dpcull_ctx ctx);
+/* Enables (default) or disables the conservative prefilter for launches made after the
+ * call (plans keep the setting they were created with).  Results are identical either
+ * way: the prefilter only decides object-views whose outcome is certain under the
+ * reference's rounding and sends all others through the exact test. */
+int dpcull_ctx_set_prefilter(dpcull_ctx ctx, int enabled);
 
 /* ---- groups: a GroupBitSet's objects and matrices resident in HBM -------------------
  * Replaces Manager::groupCreate (dp/culling/Manager.h:119). */
@@ -124,6 +129,11 @@ int dpcull_result_bits(dpcull_ctx ctx, dpcull_result r, uint32_t* out, size_t n_
                        size_t* n_bits);
 /* Manager::resultObjectIsVisible (Manager.h:132) for group index `index`. */
 int dpcull_result_is_visible(dpcull_ctx ctx, dpcull_result r, size_t index, int* visible);
+/* ResultBitSet::onNotify (ResultBitSet.cpp:110-128) for one result: the object that
+ * moved from old_index to new_index carries its visibility bit (an index past the
+ * result's size counts as visible).  For hosts that keep the group's object order
+ * themselves and re-upload objects with dpcull_group_set_objects. */
+int dpcull_result_move(dpcull_ctx ctx, dpcull_result r, size_t old_index, size_t new_index);
 /* Device pointers of r's visibility words, changed list and changed count. */
 int dpcull_result_device(dpcull_ctx ctx, dpcull_result r, uint32_t** bits, uint32_t** changed,
                          uint32_t** n_changed);

@@ -84,8 +84,11 @@ struct Result {
   uint32_t* changed = nullptr;
   size_t changed_cap = 0;
   uint32_t* n_changed = nullptr;
-  unsigned long long* status = nullptr;
-  size_t status_cap = 0;
+  uint32_t* slots = nullptr;        // tiles_cap x kTileObjects
+  uint32_t* counts = nullptr;       // tiles_cap
+  uint32_t* offsets = nullptr;      // tiles_cap
+  size_t tiles_cap = 0;
+  uint32_t n_tiles = 0;             // tiles of the group at the last prepare
 };
 
 struct TreeLaunch {
@@ -140,6 +143,7 @@ struct dpcull_ctx_s {
   int sm_count = 0;
   uint64_t launches = 0;
   uint64_t device_bytes = 0;
+  bool exact_only = false;            // prefilter disabled (testing / ablation)
   std::vector<Group> groups;
   std::vector<Result> results;
   std::vector<Tree> trees;
@@ -299,16 +303,26 @@ int result_prepare(dpcull_ctx c, Result& r, Group& g)
     if (rc) return rc;
     r.changed_cap = want;
   }
-  if (std::max<size_t>(tiles, 1) > r.status_cap) {
+  if (std::max<size_t>(tiles, 1) > r.tiles_cap) {
     CU(cudaStreamSynchronize(c->stream));
-    dfree(c, r.status, r.status_cap * 8);
-    r.status = nullptr;
-    size_t want = std::max<size_t>(tiles, r.status_cap + r.status_cap / 2);
-    int rc = dalloc(c, (void**)&r.status, want * 8);
-    if (rc) return rc;
-    CU(cudaMemsetAsync(r.status, 0, want * 8, c->stream));
-    r.status_cap = want;
+    dfree(c, r.slots, r.tiles_cap * kTileObjects * 4);
+    dfree(c, r.counts, r.tiles_cap * 4);
+    dfree(c, r.offsets, r.tiles_cap * 4);
+    r.slots = r.counts = r.offsets = nullptr;
+    const size_t want = std::max<size_t>(tiles, r.tiles_cap + r.tiles_cap / 2);
+    r.tiles_cap = 0;
+    int rc = dalloc(c, (void**)&r.slots, want * kTileObjects * 4);
+    if (!rc) rc = dalloc(c, (void**)&r.counts, want * 4);
+    if (!rc) rc = dalloc(c, (void**)&r.offsets, want * 4);
+    if (rc) {
+      dfree(c, r.slots, want * kTileObjects * 4);
+      dfree(c, r.counts, want * 4);
+      r.slots = r.counts = nullptr;
+      return rc;
+    }
+    r.tiles_cap = want;
   }
+  r.n_tiles = tiles;
   if (r.incarnation != g.incarnation) {
     r.incarnation = g.incarnation;
     const size_t old = r.size_bits;
@@ -345,7 +359,10 @@ CullView view_of(Result& r, const float* vp)
   v.bits = r.bits;
   v.changed = r.changed;
   v.n_changed = r.n_changed;
-  v.status = r.status;
+  v.slots = r.slots;
+  v.counts = r.counts;
+  v.offsets = r.offsets;
+  v.n_tiles = r.n_tiles;
   return v;
 }
 
@@ -358,17 +375,11 @@ int check_device_errors(dpcull_ctx c)
   if (err) {
     CU(cudaMemsetAsync(&c->ctl->error, 0, 2 * sizeof(unsigned int), c->stream));
     CU(cudaStreamSynchronize(c->stream));
-    if (err & kErrLookbackTimeout)
-      return fail(DPCULL_ERR_TIMEOUT, "a look-back wait expired on the device");
     if (err & kErrBadTransform)
       return fail(DPCULL_ERR_OUT_OF_RANGE, "object %u has a transform index past the matrix array", info);
   }
   return DPCULL_OK;
 }
-
-// Look-back poll budget: 2^20 polls with a 64 ns back-off, well under a second.  A tile
-// normally waits for a predecessor that is already running, a few microseconds at most.
-uint32_t spin_limit() { return 1u << 20; }
 
 int default_vpp(uint32_t max_views)
 {
@@ -428,21 +439,34 @@ int persistent_grid(dpcull_ctx c, uint32_t vpp, uint32_t ctas_per_sm, uint32_t n
   return (int)std::max<long long>(grid, 1);
 }
 
+// The cull over all scenes and views, then the changed-list assembly of every view.
 int launch_batch(dpcull_ctx c, const CullScene* d_scenes, const CullView* d_views,
-                 uint32_t n_scenes, uint32_t n_items, const dpcull_tuning& t, cudaStream_t s)
+                 uint32_t n_scenes, uint32_t n_views, uint32_t max_tiles, uint32_t n_items,
+                 const dpcull_tuning& t, cudaStream_t s)
 {
+  if (n_views > 65535) return fail(DPCULL_ERR_INVALID_ARGUMENT, "at most 65535 views per launch");
   CullLaunch a{};
   a.scenes = d_scenes;
   a.views = d_views;
   a.n_scenes = n_scenes;
   a.n_items = n_items;
   a.items_per_ticket = std::max<uint32_t>(1, t.tiles_per_ticket);
-  a.spin_limit = spin_limit();
+  a.exact_only = c->exact_only ? 1u : 0u;
   a.ctl = c->ctl;
   const int grid = persistent_grid(c, t.views_per_pass, t.ctas_per_sm, n_items, a.items_per_ticket);
   if (launch_cull(a, grid, (int)t.views_per_pass, s)) return cuda_fail(cudaGetLastError(), "cull launch");
-  c->launches++;
+  CullView none{};
+  if (launch_changed_lists(d_views, none, n_views, max_tiles, s))
+    return cuda_fail(cudaGetLastError(), "changed-list launch");
+  c->launches += 3;
   return DPCULL_OK;
+}
+
+uint32_t max_tiles_of(const std::vector<CullScene>& scenes)
+{
+  uint32_t m = 1;
+  for (auto& s : scenes) m = std::max(m, s.n_tiles);
+  return m;
 }
 
 bool valid_vpp(uint32_t v) { return v == 1 || v == 2 || v == 4 || v == 8; }
@@ -536,8 +560,6 @@ int dpcull_ctx_create(int device, void* stream, dpcull_ctx* out)
     return rc;
   }
   CullControl init{};
-  init.epoch = 1;
-  init.stride = 1;
   e = cudaMemcpy(c->ctl, &init, sizeof init, cudaMemcpyHostToDevice);
   if (e == cudaSuccess) e = cudaMallocHost((void**)&c->h_err, 2 * sizeof(unsigned int));
   if (e != cudaSuccess) {
@@ -579,6 +601,13 @@ int dpcull_ctx_synchronize(dpcull_ctx c)
 void* dpcull_ctx_stream(dpcull_ctx c) { return c ? (void*)c->stream : nullptr; }
 uint64_t dpcull_ctx_kernel_launches(dpcull_ctx c) { return c ? c->launches : 0; }
 uint64_t dpcull_ctx_device_bytes(dpcull_ctx c) { return c ? c->device_bytes : 0; }
+
+int dpcull_ctx_set_prefilter(dpcull_ctx c, int enabled)
+{
+  if (!c) return fail(DPCULL_ERR_INVALID_ARGUMENT, "null context");
+  c->exact_only = !enabled;
+  return DPCULL_OK;
+}
 
 // ---- groups ------------------------------------------------------------------------
 int dpcull_group_create(dpcull_ctx c, dpcull_group* out)
@@ -869,7 +898,9 @@ int dpcull_result_destroy(dpcull_ctx c, dpcull_result rh)
   dfree(c, r->bits, r->words_cap * 4);
   dfree(c, r->changed, r->changed_cap * 4);
   dfree(c, r->n_changed, 4);
-  dfree(c, r->status, r->status_cap * 8);
+  dfree(c, r->slots, r->tiles_cap * kTileObjects * 4);
+  dfree(c, r->counts, r->tiles_cap * 4);
+  dfree(c, r->offsets, r->tiles_cap * 4);
   if (r->group < c->groups.size()) {
     auto& v = c->groups[r->group].results;
     v.erase(std::remove(v.begin(), v.end(), rh), v.end());
@@ -897,13 +928,15 @@ int dpcull_cull(dpcull_ctx c, dpcull_group gh, dpcull_result rh, const float vp[
   a.views = nullptr;
   a.n_scenes = 1;
   a.items_per_ticket = 1;
-  a.spin_limit = spin_limit();
+  a.exact_only = c->exact_only ? 1u : 0u;
   a.ctl = c->ctl;
   a.one_scene = scene_of(*g, 0, 1, 1, 0);
   a.one_view = view_of(*r, vp);
   a.n_items = a.one_scene.n_tiles;
   if (launch_cull(a, (int)a.n_items, 1, c->stream)) return cuda_fail(cudaGetLastError(), "cull launch");
-  c->launches++;
+  if (launch_changed_lists(nullptr, a.one_view, 1, a.one_scene.n_tiles, c->stream))
+    return cuda_fail(cudaGetLastError(), "changed-list launch");
+  c->launches += 3;
   return DPCULL_OK;
 }
 
@@ -958,6 +991,18 @@ int dpcull_result_is_visible(dpcull_ctx c, dpcull_result rh, size_t index, int* 
   return DPCULL_OK;
 }
 
+int dpcull_result_move(dpcull_ctx c, dpcull_result rh, size_t old_index, size_t new_index)
+{
+  Result* r = get_result(c, rh);
+  if (!r) return fail(DPCULL_ERR_INVALID_ARGUMENT, "bad result %u", rh);
+  if (!r->bits || new_index >= r->size_bits) return DPCULL_OK;
+  const uint32_t old32 = old_index >= r->size_bits ? (uint32_t)r->size_bits : (uint32_t)old_index;
+  if (launch_move_bit(r->bits, (uint32_t)r->size_bits, old32, (uint32_t)new_index, c->stream))
+    return cuda_fail(cudaGetLastError(), "move bit");
+  c->launches++;
+  return DPCULL_OK;
+}
+
 int dpcull_result_device(dpcull_ctx c, dpcull_result rh, uint32_t** bits, uint32_t** changed,
                          uint32_t** n_changed)
 {
@@ -994,7 +1039,8 @@ int dpcull_cull_batched(dpcull_ctx c, const dpcull_job* jobs, size_t n_jobs, con
   }
   cudaMemcpyAsync(ds, scenes.data(), scenes.size() * sizeof(CullScene), cudaMemcpyHostToDevice, c->stream);
   cudaMemcpyAsync(dv, views.data(), views.size() * sizeof(CullView), cudaMemcpyHostToDevice, c->stream);
-  rc = launch_batch(c, ds, dv, (uint32_t)scenes.size(), items, t, c->stream);
+  rc = launch_batch(c, ds, dv, (uint32_t)scenes.size(), (uint32_t)views.size(), max_tiles_of(scenes),
+                    items, t, c->stream);
   cudaStreamSynchronize(c->stream);
   dfree(c, ds, scenes.size() * sizeof(CullScene));
   dfree(c, dv, views.size() * sizeof(CullView));
@@ -1013,7 +1059,8 @@ static int plan_capture(dpcull_ctx c, Plan& p, int slot)
   int rc = DPCULL_OK;
   if (e == cudaSuccess) {
     const uint64_t before = c->launches;
-    rc = launch_batch(c, p.d_scenes, p.d_views, (uint32_t)p.scenes.size(), p.n_items, p.tuning, cs);
+    rc = launch_batch(c, p.d_scenes, p.d_views, (uint32_t)p.scenes.size(), (uint32_t)p.views.size(),
+                      max_tiles_of(p.scenes), p.n_items, p.tuning, cs);
     c->launches = before;  // counted when the graph is replayed
   }
   cudaError_t e2 = cudaStreamEndCapture(cs, &graph);
@@ -1026,15 +1073,17 @@ static int plan_capture(dpcull_ctx c, Plan& p, int slot)
   return DPCULL_OK;
 }
 
-static int time_batch(dpcull_ctx c, const CullScene* ds, const CullView* dv, uint32_t n_scenes,
+static int time_batch(dpcull_ctx c, const CullScene* ds, const CullView* dv,
+                      const std::vector<CullScene>& sc, const std::vector<CullView>& vw,
                       uint32_t items, const dpcull_tuning& t, int reps, float* ms)
 {
   cudaEvent_t e0, e1;
   CU(cudaEventCreate(&e0));
   CU(cudaEventCreate(&e1));
-  int rc = launch_batch(c, ds, dv, n_scenes, items, t, c->stream);  // warm-up
+  const uint32_t ns = (uint32_t)sc.size(), nvw = (uint32_t)vw.size(), mt = max_tiles_of(sc);
+  int rc = launch_batch(c, ds, dv, ns, nvw, mt, items, t, c->stream);  // warm-up
   if (!rc) cudaEventRecord(e0, c->stream);
-  for (int i = 0; i < reps && !rc; ++i) rc = launch_batch(c, ds, dv, n_scenes, items, t, c->stream);
+  for (int i = 0; i < reps && !rc; ++i) rc = launch_batch(c, ds, dv, ns, nvw, mt, items, t, c->stream);
   if (!rc) {
     cudaEventRecord(e1, c->stream);
     cudaEventSynchronize(e1);
@@ -1096,7 +1145,7 @@ int dpcull_autotune(dpcull_ctx c, const dpcull_job* jobs, size_t n_jobs, dpcull_
       for (int cps = 1; cps <= occ; ++cps) {
         dpcull_tuning t{vpp, tpt, (uint32_t)cps, 0};
         float ms = 0;
-        rc = time_batch(c, ds, dv, (uint32_t)sc.size(), it_items, t, 3, &ms);
+        rc = time_batch(c, ds, dv, sc, vw, it_items, t, 3, &ms);
         if (rc) break;
         if (ms < best_ms) {
           best_ms = ms;

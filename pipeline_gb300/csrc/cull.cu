@@ -4,16 +4,22 @@
 // CTA per tile) and the batched persistent path (many groups x many views, a grid of
 // resident CTAs that pull work items from an atomic ticket).  A work item is one tile of
 // 1024 objects of one scene and one group of up to VPP views:
-//   1. stage the views' view-projection matrices in shared memory;
+//   1. stage the views' view-projection matrices (and their prefilter bounds) in shared
+//      memory;
 //   2. 128-bit streaming loads of the tile's SoA rows (each thread owns 4 objects);
-//   3. per object: gather its world matrix (4 x 128-bit __ldg), build the world-space box
-//      exactly as the reference's OBB cache, and run the exact clip test once per view;
+//   3. per object: gather its world matrix (4 x 128-bit __ldg) and build the world-space
+//      box exactly as the reference's OBB cache; per view, the conservative prefilter
+//      (dpcull_exact.cuh) decides visible / invisible where the reference's rounded
+//      result is certain; the undecided (object, view) pairs of the tile are compacted
+//      into a shared-memory queue and run through the exact reference test by all
+//      threads together, so no warp idles on a rare exact pair;
 //   4. per view: assemble the 32-bit visibility words with warp shuffles, XOR them with
-//      the result's previous words (ResultBitSet::updateChanged), write the new words,
-//      and place the changed objects in the global ascending list with a single-pass
-//      decoupled look-back over the tiles of that scene and view.
-// Every wait on another tile is bounded; on expiry the kernel sets an error bit, still
-// publishes its status (so no successor waits forever) and the host reports the error.
+//      the result's previous words (ResultBitSet::updateChanged), write the new words
+//      (only where they changed), and write the tile's changed objects, ascending, into
+//      the tile's private slot range together with the tile's count.
+// A CTA never waits for another.  Two small kernels then turn the per-tile slots into
+// the packed ascending changed list: a per-view exclusive scan of the tile counts and a
+// gather of the slots (launch_changed_lists).
 #include <cuda_runtime.h>
 
 #include "dpcull_exact.cuh"
@@ -22,18 +28,6 @@
 namespace dpcull {
 
 namespace {
-
-__device__ __forceinline__ unsigned long long ld_relaxed_u64(const unsigned long long* p)
-{
-  unsigned long long v;
-  asm volatile("ld.relaxed.gpu.global.u64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
-  return v;
-}
-
-__device__ __forceinline__ void st_relaxed_u64(unsigned long long* p, unsigned long long v)
-{
-  asm volatile("st.relaxed.gpu.global.u64 [%0], %1;" ::"l"(p), "l"(v) : "memory");
-}
 
 __device__ __forceinline__ float4 ld_stream4(const float* p)
 {
@@ -55,69 +49,14 @@ __device__ __forceinline__ uint32_t compu(const uint4& v, int k)
   return k == 0 ? v.x : k == 1 ? v.y : k == 2 ? v.z : v.w;
 }
 
-__device__ __forceinline__ unsigned long long pack_status(uint32_t epoch, uint32_t flag,
-                                                          uint32_t value)
-{
-  return ((unsigned long long)epoch << 32) | ((unsigned long long)flag << 30) |
-         (unsigned long long)(value & 0x3FFFFFFFu);
-}
-
-// Warp-cooperative decoupled look-back.  Publishes this tile's aggregate, sums the
-// aggregates of its predecessors (32 at a time) until it meets an inclusive prefix,
-// publishes its own inclusive prefix and returns the exclusive prefix (lane-uniform).
-__device__ uint32_t lookback(unsigned long long* status, uint32_t tile, uint32_t total,
-                             uint32_t epoch, uint32_t spin_limit, CullControl* ctl)
-{
-  const int lane = threadIdx.x & 31;
-  if (tile == 0) {
-    if (lane == 0) st_relaxed_u64(&status[0], pack_status(epoch, kFlagPrefix, total));
-    return 0;
-  }
-  if (lane == 0) st_relaxed_u64(&status[tile], pack_status(epoch, kFlagAggregate, total));
-  uint32_t excl = 0;
-  int64_t top = (int64_t)tile - 1;
-  uint32_t polls = 0;
-  bool timed_out = false;
-  for (;;) {
-    const int64_t pred = top - lane;
-    unsigned long long s;
-    for (;;) {
-      s = pred >= 0 ? ld_relaxed_u64(&status[pred]) : pack_status(epoch, kFlagPrefix, 0);
-      const bool ready = (uint32_t)(s >> 32) == epoch && ((s >> 30) & 3u) != 0;
-      if (__all_sync(0xffffffffu, ready)) break;
-      // Give up when the budget is spent, or at once when another tile already gave up
-      // (then no wait in this launch can be trusted and none may run its full budget).
-      if (++polls > spin_limit ||
-          ((polls & 255u) == 0 &&
-           (*reinterpret_cast<volatile unsigned int*>(&ctl->error) & kErrLookbackTimeout))) {
-        timed_out = true;
-        break;
-      }
-      __nanosleep(64);
-    }
-    if (timed_out) break;
-    const uint32_t flag = (uint32_t)(s >> 30) & 3u;
-    const uint32_t val = (uint32_t)s & 0x3FFFFFFFu;
-    const uint32_t pmask = __ballot_sync(0xffffffffu, flag == kFlagPrefix);
-    if (pmask) {
-      const int first = __ffs(pmask) - 1;
-      excl += __reduce_add_sync(0xffffffffu, lane <= first ? val : 0u);
-      break;
-    }
-    excl += __reduce_add_sync(0xffffffffu, val);
-    top -= 32;
-  }
-  if (timed_out && lane == 0) atomicOr(&ctl->error, kErrLookbackTimeout);
-  // Publish even after a timeout so that no successor waits on this tile.
-  if (lane == 0) st_relaxed_u64(&status[tile], pack_status(epoch, kFlagPrefix, excl + total));
-  return excl;
-}
-
 struct CullShared {
   float vp[kMaxViewsPerPass][16];
+  float4 vn[kMaxViewsPerPass];                       // prefilter view bounds
+  uint32_t vis[kMaxViewsPerPass][kTileWords];        // visibility from the exact drain
   uint32_t wtot[kMaxViewsPerPass][kThreads / 32];   // per-warp changed counts
-  uint32_t wbase[kMaxViewsPerPass][kThreads / 32];  // per-warp output offsets
   uint32_t item;
+  uint32_t qn;                                       // undecided (object, view) pairs
+  uint16_t queue[kTileObjects * kMaxViewsPerPass];   // entry = tile object << 3 | view
 };
 
 __device__ __forceinline__ uint32_t find_scene(const CullScene* scenes, uint32_t n, uint32_t item)
@@ -131,8 +70,23 @@ __device__ __forceinline__ uint32_t find_scene(const CullScene* scenes, uint32_t
   return lo;
 }
 
-template <int VPP>
-__device__ void process_item(const CullLaunch& a, uint32_t item, uint32_t epoch, CullShared& sh)
+// Exact visibility of one object of the scene (reference operation order), reloading its
+// row and matrix; used for the pairs the prefilter cannot decide.
+__device__ __forceinline__ bool exact_visible(const CullScene& sc, uint32_t i, const float* vp)
+{
+  const float* soa = sc.soa;
+  const size_t cap = sc.cap;
+  const uint32_t mi = __ldg(reinterpret_cast<const uint32_t*>(soa) + 6 * cap + i);
+  const float4* M = reinterpret_cast<const float4*>(sc.mats) + 4 * (size_t)mi;
+  const Obb o = make_obb(__ldg(soa + i), __ldg(soa + cap + i), __ldg(soa + 2 * cap + i),
+                         __ldg(soa + 3 * cap + i), __ldg(soa + 4 * cap + i),
+                         __ldg(soa + 5 * cap + i), __ldg(M + 0), __ldg(M + 1), __ldg(M + 2),
+                         __ldg(M + 3));
+  return obb_visible(o, vp);
+}
+
+template <int VPP, bool PF>
+__device__ void process_item(const CullLaunch& a, uint32_t item, CullShared& sh)
 {
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const CullScene sc = a.scenes ? a.scenes[find_scene(a.scenes, a.n_scenes, item)] : a.one_scene;
@@ -143,7 +97,15 @@ __device__ void process_item(const CullLaunch& a, uint32_t item, uint32_t epoch,
   const CullView* views = a.views ? a.views + sc.view_begin + vfirst : &a.one_view;
 
   if (tid < nv * 16) sh.vp[tid >> 4][tid & 15] = views[tid >> 4].vp[tid & 15];
+  if (PF) {
+    if (tid < VPP * kTileWords) sh.vis[tid / kTileWords][tid % kTileWords] = 0u;
+    if (tid == 0) sh.qn = 0u;
+  }
   __syncthreads();
+  if (PF) {
+    if (tid < nv) sh.vn[tid] = pf_view(sh.vp[tid]);
+    __syncthreads();
+  }
 
   // ---- visibility of my 4 objects in each view ----
   const uint32_t obj0 = tile * kTileObjects + (uint32_t)tid * kObjPerThread;
@@ -161,6 +123,7 @@ __device__ void process_item(const CullLaunch& a, uint32_t item, uint32_t epoch,
   uint32_t nib[VPP];
 #pragma unroll
   for (int v = 0; v < VPP; ++v) nib[v] = 0;
+  uint32_t amb = 0;  // bit 8k + v: object k in view v needs the exact test
 
 #pragma unroll
   for (int k = 0; k < kObjPerThread; ++k) {
@@ -171,13 +134,58 @@ __device__ void process_item(const CullLaunch& a, uint32_t item, uint32_t epoch,
         const float4 r0 = __ldg(M + 0), r1 = __ldg(M + 1), r2 = __ldg(M + 2), r3 = __ldg(M + 3);
         const Obb o = make_obb(comp(lx, k), comp(ly, k), comp(lz, k), comp(ex, k), comp(ey, k),
                                comp(ez, k), r0, r1, r2, r3);
+        if (PF) {
+          const PfObject b = pf_object(o);
 #pragma unroll
-        for (int v = 0; v < VPP; ++v)
-          if (v < nv && obb_visible(o, sh.vp[v])) nib[v] |= 1u << k;
+          for (int v = 0; v < VPP; ++v) {
+            if (v < nv) {
+              const int cls = pf_classify(b, sh.vp[v], sh.vn[v]);
+              if (cls == kPfVisible) nib[v] |= 1u << k;
+              else if (cls == kPfAmbiguous) amb |= 1u << (8 * k + v);
+            }
+          }
+        } else {
+#pragma unroll
+          for (int v = 0; v < VPP; ++v)
+            if (v < nv && obb_visible(o, sh.vp[v])) nib[v] |= 1u << k;
+        }
       } else {
         if (atomicOr(&a.ctl->error, kErrBadTransform) == 0) a.ctl->error_info = obj0 + k;
       }
     }
+  }
+
+  if (PF) {
+    // ---- compact the undecided pairs of the tile and run them through the exact test ----
+    const uint32_t cnt = (uint32_t)__popc(amb);
+    uint32_t x = cnt;
+#pragma unroll
+    for (int d = 1; d < 32; d <<= 1) {
+      const uint32_t y = __shfl_up_sync(0xffffffffu, x, d);
+      if (lane >= d) x += y;
+    }
+    uint32_t base = 0;
+    if (lane == 31) base = atomicAdd(&sh.qn, x);
+    base = __shfl_sync(0xffffffffu, base, 31);
+    uint32_t pos = base + x - cnt;
+    while (amb) {
+      const int b = __ffs(amb) - 1;
+      sh.queue[pos++] =
+          (uint16_t)(((uint32_t)(tid * kObjPerThread + (b >> 3)) << 3) | (uint32_t)(b & 7));
+      amb &= amb - 1u;
+    }
+    __syncthreads();
+    const uint32_t qn = sh.qn;
+    const uint32_t tile0 = tile * kTileObjects;
+    for (uint32_t q = tid; q < qn; q += kThreads) {
+      const uint32_t e = sh.queue[q];
+      const uint32_t o = e >> 3, v = e & 7u;
+      if (exact_visible(sc, tile0 + o, sh.vp[v])) atomicOr(&sh.vis[v][o >> 5], 1u << (o & 31));
+    }
+    __syncthreads();
+#pragma unroll
+    for (int v = 0; v < VPP; ++v)
+      if (v < nv) nib[v] |= (sh.vis[v][tid >> 3] >> ((tid & 7) * 4)) & 0xFu;
   }
 
   // ---- words, changed nibbles and per-thread changed counts ----
@@ -190,7 +198,7 @@ __device__ void process_item(const CullLaunch& a, uint32_t item, uint32_t epoch,
 #pragma unroll
   for (int v = 0; v < VPP; ++v) {
     chg[v] = 0;
-    if (v < nv) {
+    if (v < nv) {  // nv is uniform over the CTA, so the shuffles stay warp-uniform
       uint32_t* bits = views[v].bits;
       const uint32_t prev = bits[word];
       chg[v] = nib[v] ^ ((prev >> shift) & 0xFu);
@@ -200,8 +208,6 @@ __device__ void process_item(const CullLaunch& a, uint32_t item, uint32_t epoch,
       w |= __shfl_xor_sync(0xffffffffu, w, 4);
       if ((tid & 7) == 0 && w != prev) bits[word] = w;
       packed[v >> 2] |= (uint32_t)__popc(chg[v]) << (8 * (v & 3));
-    } else {
-      // keep the shuffles warp-uniform: nv is uniform, so this branch is too
     }
   }
 
@@ -224,47 +230,39 @@ __device__ void process_item(const CullLaunch& a, uint32_t item, uint32_t epoch,
   }
   __syncthreads();
 
-  // ---- tile totals and look-back: warp v handles view v ----
-  if (warp < nv) {
-    const int v = warp;
-    uint32_t x = lane < kThreads / 32 ? sh.wtot[v][lane] : 0u;
-    const uint32_t own = x;
-#pragma unroll
-    for (int d = 1; d < kThreads / 32; d <<= 1) {
-      const uint32_t y = __shfl_up_sync(0xffffffffu, x, d);
-      if (lane >= d) x += y;
-    }
-    const uint32_t total = __shfl_sync(0xffffffffu, x, kThreads / 32 - 1);
-    const uint32_t base = lookback(views[v].status, tile, total, epoch, a.spin_limit, a.ctl);
-    if (lane < kThreads / 32) sh.wbase[v][lane] = base + x - own;
-    if (lane == 0 && tile == sc.n_tiles - 1) *views[v].n_changed = base + total;
-  }
-  __syncthreads();
-
-  // ---- ascending changed-object indices ----
+  // ---- the tile's changed objects, ascending, into its private slots ----
 #pragma unroll
   for (int v = 0; v < VPP; ++v) {
-    if (v < nv && chg[v]) {
-      const uint32_t own = (uint32_t)__popc(chg[v]);
-      uint32_t off = sh.wbase[v][warp] + ((incl[v >> 2] >> (8 * (v & 3))) & 0xFFu) - own;
-      uint32_t* out = views[v].changed;
-      uint32_t m = chg[v];
-      while (m) {
-        const int k = __ffs(m) - 1;
-        out[off++] = obj0 + (uint32_t)k;
-        m &= m - 1u;
+    if (v < nv) {
+      uint32_t before = 0, total = 0;
+#pragma unroll
+      for (int w = 0; w < kThreads / 32; ++w) {
+        const uint32_t t = sh.wtot[v][w];
+        before += w < warp ? t : 0u;
+        total += t;
+      }
+      if (tid == 0) views[v].counts[tile] = total;
+      if (chg[v]) {
+        const uint32_t own = (uint32_t)__popc(chg[v]);
+        uint32_t off = tile * kTileObjects + before + ((incl[v >> 2] >> (8 * (v & 3))) & 0xFFu) - own;
+        uint32_t* slots = views[v].slots;
+        uint32_t m = chg[v];
+        while (m) {
+          const int k = __ffs(m) - 1;
+          slots[off++] = obj0 + (uint32_t)k;
+          m &= m - 1u;
+        }
       }
     }
   }
   __syncthreads();  // shared views / totals are reused by the next item
 }
 
-template <int VPP>
+template <int VPP, bool PF>
 __global__ void __launch_bounds__(kThreads) cull_kernel(const __grid_constant__ CullLaunch a)
 {
   __shared__ CullShared sh;
   CullControl* ctl = a.ctl;
-  const uint32_t epoch = *reinterpret_cast<volatile unsigned int*>(&ctl->epoch);
   for (;;) {
     if (threadIdx.x == 0) sh.item = atomicAdd(&ctl->ticket, a.items_per_ticket);
     __syncthreads();
@@ -272,26 +270,81 @@ __global__ void __launch_bounds__(kThreads) cull_kernel(const __grid_constant__ 
     __syncthreads();
     if (first >= a.n_items) break;
     const uint32_t last = min(first + a.items_per_ticket, a.n_items);
-    for (uint32_t item = first; item < last; ++item) process_item<VPP>(a, item, epoch, sh);
+    for (uint32_t item = first; item < last; ++item) process_item<VPP, PF>(a, item, sh);
   }
   if (threadIdx.x == 0) {
     __threadfence();
     const unsigned int prev = atomicAdd(&ctl->done, 1u);
     if (prev == gridDim.x - 1) {
-      // Last CTA of the launch: reset the ticket and advance the epoch, so the next
-      // launch on this control block needs no memset.
+      // Last CTA of the launch: reset the ticket for the next launch (no memset needed).
       ctl->ticket = 0;
       ctl->done = 0;
-      __threadfence();
-      atomicAdd(&ctl->epoch, ctl->stride);
     }
+  }
+}
+
+// ---- changed-list assembly ----------------------------------------------------------------
+constexpr int kScanThreads = 1024;
+
+// One CTA per view: exclusive scan of the tile counts into offsets, total into n_changed.
+__global__ void __launch_bounds__(kScanThreads)
+    scan_counts_kernel(const CullView* views, const __grid_constant__ CullView one)
+{
+  __shared__ uint32_t warp_sum[kScanThreads / 32];
+  const CullView& v = views ? views[blockIdx.x] : one;
+  const uint32_t n = v.n_tiles;
+  const uint32_t per = (n + kScanThreads - 1) / kScanThreads;
+  const uint32_t b = min(n, threadIdx.x * per), e = min(n, b + per);
+  uint32_t s = 0;
+  for (uint32_t i = b; i < e; ++i) s += v.counts[i];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  uint32_t x = s;
+#pragma unroll
+  for (int d = 1; d < 32; d <<= 1) {
+    const uint32_t y = __shfl_up_sync(0xffffffffu, x, d);
+    if (lane >= d) x += y;
+  }
+  if (lane == 31) warp_sum[warp] = x;
+  __syncthreads();
+  if (warp == 0) {
+    uint32_t w = warp_sum[lane];
+#pragma unroll
+    for (int d = 1; d < 32; d <<= 1) {
+      const uint32_t y = __shfl_up_sync(0xffffffffu, w, d);
+      if (lane >= d) w += y;
+    }
+    warp_sum[lane] = w;  // inclusive over warps
+  }
+  __syncthreads();
+  uint32_t run = (warp ? warp_sum[warp - 1] : 0u) + x - s;
+  for (uint32_t i = b; i < e; ++i) {
+    const uint32_t c = v.counts[i];
+    v.offsets[i] = run;
+    run += c;
+  }
+  if (threadIdx.x == kScanThreads - 1) *v.n_changed = warp_sum[31];
+}
+
+// blockIdx.y = view; each warp copies whole tiles' slot ranges to their packed position.
+__global__ void gather_changed_kernel(const CullView* views, const __grid_constant__ CullView one)
+{
+  const CullView& v = views ? views[blockIdx.y] : one;
+  const int lane = threadIdx.x & 31;
+  const uint32_t warps = blockDim.x / 32;
+  for (uint32_t t = blockIdx.x * warps + threadIdx.x / 32; t < v.n_tiles; t += gridDim.x * warps) {
+    const uint32_t c = v.counts[t];
+    if (!c) continue;
+    const uint32_t o = v.offsets[t];
+    const uint32_t* src = v.slots + (size_t)t * kTileObjects;
+    for (uint32_t j = lane; j < c; j += 32) v.changed[o + j] = src[j];
   }
 }
 
 template <int VPP>
 int launch_vpp(const CullLaunch& a, int grid, cudaStream_t s)
 {
-  cull_kernel<VPP><<<grid, kThreads, 0, s>>>(a);
+  if (a.exact_only) cull_kernel<VPP, false><<<grid, kThreads, 0, s>>>(a);
+  else cull_kernel<VPP, true><<<grid, kThreads, 0, s>>>(a);
   return cudaGetLastError() == cudaSuccess ? 0 : -1;
 }
 
@@ -299,7 +352,7 @@ template <int VPP>
 int max_ctas()
 {
   int n = 0;
-  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, cull_kernel<VPP>, kThreads, 0) != cudaSuccess)
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, cull_kernel<VPP, true>, kThreads, 0) != cudaSuccess)
     return 1;
   return n > 0 ? n : 1;
 }
@@ -347,6 +400,20 @@ int cull_max_ctas_per_sm(int vpp)
     case 8: return max_ctas<8>();
     default: return 1;
   }
+}
+
+int launch_changed_lists(const CullView* views, const CullView& one, uint32_t n_views,
+                         uint32_t max_tiles, void* stream)
+{
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  if (!n_views) return 0;
+  scan_counts_kernel<<<n_views, kScanThreads, 0, s>>>(views, one);
+  const uint32_t warps = 8;
+  uint32_t gx = (max_tiles + warps - 1) / warps;
+  if (gx > 64) gx = 64;
+  if (gx < 1) gx = 1;
+  gather_changed_kernel<<<dim3(gx, n_views), warps * 32, 0, s>>>(views, one);
+  return cudaGetLastError() == cudaSuccess ? 0 : -1;
 }
 
 int launch_move_bit(uint32_t* bits, uint32_t size_bits, uint32_t old_index, uint32_t new_index,

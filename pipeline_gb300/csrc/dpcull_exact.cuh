@@ -114,4 +114,106 @@ __device__ __forceinline__ bool obb_visible(const Obb& o, const float* vp)
   return acc.visible();
 }
 
+// ---------------------------------------------------------------------------------------
+// Conservative classification that never contradicts obb_visible().
+//
+// Let p, ex, ey, ez be the (float) box of make_obb and C_k = p + s ex + t ey + u ez the
+// 8 exact real corners; obb_visible() evaluates rounded corners c_k.  For the clip plane
+// "lo a" (a = x, y, z) the reference tests c_a <= -c_w, i.e. c_a + c_w <= 0, and for
+// "hi a" it tests !(c_a <= -c_w) && c_w <= c_a.  With col_j column j of VP,
+// Pi = col_a + col_w (lo) or col_w - col_a (hi), and B_a[i] = |col_a[i]| + |col_w[i]|:
+//   * rounding: |(c_a + c_w) - (C_a + C_w)| <= 7u * sum_i a_i B_a[i] <= 7u * A * N_a,
+//     u = 2^-24, a_i = |p_i|+|ex_i|+|ey_i|+|ez_i|, A = ||a||_2, N_a = ||B_a||_2
+//     (4-term dot products plus the 3-add corner chain, Cauchy-Schwarz);
+//   * extent: over the 8 corners, C.Pi lies within centre.Pi +- R N_a, centre =
+//     p + (ex+ey+ez)/2, R = (||ex||+||ey||+||ez||)/2, since |e.Pi| <= ||e|| N_a;
+//   * this test: L = fl(cc_a + cc_w) with cc = fl(centre' . VP) (FMA chains, centre'
+//     rounded) is within 9u * A * N_a of centre.Pi.
+// So with T_a >= (R + 16u A) N_a: L <= -T_a proves every rounded corner is outside
+// "lo a" (the cfa bit is set: invisible); L_hi <= -T_a && L_lo > T_a proves every
+// corner outside "hi a" (invisible); L_lo > T_a && L_hi > T_a for all three axes proves
+// every corner strictly inside (cf = 0: visible).  Anything else is ambiguous and goes
+// through obb_visible().  T_a uses delta = 2^-19 = 32u instead of 16u, and K and N_a are
+// inflated by 2^-18 to cover the rounding of the norms; eta = 2^-120 absorbs subnormal
+// rounding.  The bounds need finite values without overflow: a box with A >= 2^50 or a
+// view whose N_a is not finite and below 2^50 gets K or N = NaN, so every comparison
+// fails and the pair is ambiguous (then |terms| <= A N_a < 2^100: no overflow anywhere).
+constexpr float kPfDelta = 0x1p-19f;
+constexpr float kPfInflate = 1.0f + 0x1p-18f;
+constexpr float kPfEta = 0x1p-120f;
+constexpr float kPfLimit = 0x1p50f;
+
+struct PfObject {
+  float4 c;  // box centre
+  float K;   // (R + delta A) inflated, NaN when the bounds do not apply
+};
+
+__device__ __forceinline__ float norm4(float4 v)
+{
+  return sqrtf(fmaf(v.x, v.x, fmaf(v.y, v.y, fmaf(v.z, v.z, v.w * v.w))));
+}
+
+__device__ __forceinline__ PfObject pf_object(const Obb& o)
+{
+  PfObject b;
+  b.c = make_float4(fmaf(0.5f, o.ez.x, fmaf(0.5f, o.ey.x, fmaf(0.5f, o.ex.x, o.p.x))),
+                    fmaf(0.5f, o.ez.y, fmaf(0.5f, o.ey.y, fmaf(0.5f, o.ex.y, o.p.y))),
+                    fmaf(0.5f, o.ez.z, fmaf(0.5f, o.ey.z, fmaf(0.5f, o.ex.z, o.p.z))),
+                    fmaf(0.5f, o.ez.w, fmaf(0.5f, o.ey.w, fmaf(0.5f, o.ex.w, o.p.w))));
+  const float4 a = make_float4(fabsf(o.p.x) + fabsf(o.ex.x) + fabsf(o.ey.x) + fabsf(o.ez.x),
+                               fabsf(o.p.y) + fabsf(o.ex.y) + fabsf(o.ey.y) + fabsf(o.ez.y),
+                               fabsf(o.p.z) + fabsf(o.ex.z) + fabsf(o.ey.z) + fabsf(o.ez.z),
+                               fabsf(o.p.w) + fabsf(o.ex.w) + fabsf(o.ey.w) + fabsf(o.ez.w));
+  const float A = norm4(a);
+  const float R = 0.5f * (norm4(o.ex) + norm4(o.ey) + norm4(o.ez));
+  b.K = A < kPfLimit ? fmaf(kPfDelta, A, R) * kPfInflate : __int_as_float(0x7fffffff);
+  return b;
+}
+
+// Per-view N_x, N_y, N_z (inflated), NaN when the view is not finite or too large.
+__device__ __forceinline__ float4 pf_view(const float* vp)
+{
+  float n[3] = {0.f, 0.f, 0.f};
+  bool ok = true;
+#pragma unroll
+  for (int i = 0; i < 4; ++i) {
+    const float w = fabsf(vp[4 * i + 3]);
+    ok &= isfinite(vp[4 * i + 3]);
+#pragma unroll
+    for (int j = 0; j < 3; ++j) {
+      ok &= isfinite(vp[4 * i + j]);
+      const float b = fabsf(vp[4 * i + j]) + w;
+      n[j] = fmaf(b, b, n[j]);
+    }
+  }
+  float4 r = make_float4(sqrtf(n[0]) * kPfInflate, sqrtf(n[1]) * kPfInflate,
+                         sqrtf(n[2]) * kPfInflate, 0.f);
+  ok &= r.x < kPfLimit && r.y < kPfLimit && r.z < kPfLimit;
+  if (!ok) r = make_float4(__int_as_float(0x7fffffff), __int_as_float(0x7fffffff),
+                           __int_as_float(0x7fffffff), 0.f);
+  return r;
+}
+
+enum : int { kPfInvisible = 0, kPfVisible = 1, kPfAmbiguous = 2 };
+
+__device__ __forceinline__ int pf_classify(const PfObject& b, const float* vp, float4 vn)
+{
+  const float4 r0 = *reinterpret_cast<const float4*>(vp + 0);
+  const float4 r1 = *reinterpret_cast<const float4*>(vp + 4);
+  const float4 r2 = *reinterpret_cast<const float4*>(vp + 8);
+  const float4 r3 = *reinterpret_cast<const float4*>(vp + 12);
+  const float cx = fmaf(b.c.w, r3.x, fmaf(b.c.z, r2.x, fmaf(b.c.y, r1.x, b.c.x * r0.x)));
+  const float cy = fmaf(b.c.w, r3.y, fmaf(b.c.z, r2.y, fmaf(b.c.y, r1.y, b.c.x * r0.y)));
+  const float cz = fmaf(b.c.w, r3.z, fmaf(b.c.z, r2.z, fmaf(b.c.y, r1.z, b.c.x * r0.z)));
+  const float cw = fmaf(b.c.w, r3.w, fmaf(b.c.z, r2.w, fmaf(b.c.y, r1.w, b.c.x * r0.w)));
+  const float tx = fmaf(b.K, vn.x, kPfEta), ty = fmaf(b.K, vn.y, kPfEta), tz = fmaf(b.K, vn.z, kPfEta);
+  const float lox = cx + cw, hix = cw - cx;
+  const float loy = cy + cw, hiy = cw - cy;
+  const float loz = cz + cw, hiz = cw - cz;
+  const bool out = (lox <= -tx) | ((hix <= -tx) & (lox > tx)) | (loy <= -ty) |
+                   ((hiy <= -ty) & (loy > ty)) | (loz <= -tz) | ((hiz <= -tz) & (loz > tz));
+  const bool in = (lox > tx) & (hix > tx) & (loy > ty) & (hiy > ty) & (loz > tz) & (hiz > tz);
+  return out ? kPfInvisible : (in ? kPfVisible : kPfAmbiguous);
+}
+
 }  // namespace dpcull

@@ -7,8 +7,10 @@
 // load of a tile stays inside the allocation.  World matrices are Mat44f rows
 // (4 x float4, row-major, row-vector convention) gathered by transform index.
 // A result (one group x one view) owns its visibility bit array (bit i of word i/32 is
-// object i, the ResultBitSet layout), its changed-object list and its look-back status
-// words (one per tile).
+// object i, the ResultBitSet layout), its changed-object list and its scratch: one
+// changed count per tile, the tiles' exclusive offsets, and a tile-private slot range of
+// kTileObjects indices per tile (the cull writes each tile's changed objects there; a
+// scan of the counts and a gather then build the packed ascending list).
 #pragma once
 
 #include <cstddef>
@@ -21,15 +23,10 @@ constexpr int kObjPerThread = 4;                   // one float4 of each SoA row
 constexpr int kTileObjects = kThreads * kObjPerThread;  // 1024 objects per tile
 constexpr int kTileWords = kTileObjects / 32;      // 32 bit-array words per tile and view
 constexpr int kMaxViewsPerPass = 8;                // views evaluated per object load
-constexpr uint32_t kMaxObjects = (1u << 30) - 1;   // changed counts are packed in 30 bits
-
-// Look-back status word: epoch (32) | flag (2) | value (30).
-constexpr uint32_t kFlagAggregate = 1;
-constexpr uint32_t kFlagPrefix = 2;
+constexpr uint32_t kMaxObjects = (1u << 30) - 1;   // keeps every index and count in 32 bits
 
 // Error bits reported through CullControl::error.
 constexpr uint32_t kErrBadTransform = 1u;   // transform index >= matrix count
-constexpr uint32_t kErrLookbackTimeout = 2u; // bounded wait for a predecessor tile expired
 
 struct CullScene {
   const float* soa;        // base of the group's SoA block
@@ -46,20 +43,21 @@ struct CullScene {
 
 struct CullView {
   float vp[16];
-  uint32_t* bits;                 // previous visibility on entry, new visibility on exit
-  uint32_t* changed;              // ascending changed-object list
-  uint32_t* n_changed;            // total, written by the scene's last tile
-  unsigned long long* status;     // one look-back word per tile
+  uint32_t* bits;        // previous visibility on entry, new visibility on exit
+  uint32_t* changed;     // ascending changed-object list
+  uint32_t* n_changed;   // its length
+  uint32_t* slots;       // scratch: kTileObjects changed indices per tile
+  uint32_t* counts;      // scratch: changed objects per tile
+  uint32_t* offsets;     // scratch: exclusive prefix of counts
+  uint32_t n_tiles;
+  uint32_t pad;
 };
 
 struct CullControl {
   unsigned int ticket;     // next work item
   unsigned int done;       // CTAs finished
-  unsigned int epoch;      // current launch's epoch (advanced by the last CTA)
-  unsigned int stride;     // epoch increment (distinct per control block)
   unsigned int error;      // sticky kErr* bits
   unsigned int error_info; // first offending index
-  unsigned int pad[2];
 };
 
 struct CullLaunch {
@@ -68,7 +66,7 @@ struct CullLaunch {
   uint32_t n_scenes;
   uint32_t n_items;
   uint32_t items_per_ticket; // tiles claimed per ticket ("tiles per CTA" tuning knob)
-  uint32_t spin_limit;       // look-back wait budget (polls)
+  uint32_t exact_only;       // 1 = skip the conservative prefilter (every pair exact)
   CullControl* ctl;
   CullScene one_scene;
   CullView one_view;
@@ -77,6 +75,11 @@ struct CullLaunch {
 // Launchers (cull.cu).  vpp = views per pass (1, 2, 4 or 8).
 int launch_cull(const CullLaunch& args, int grid, int vpp, void* stream);
 int cull_max_ctas_per_sm(int vpp);
+// Changed-list assembly after a cull launch over `n_views` views (device array `views`,
+// or the single `one` when views is null): per-view scan of the tile counts, then the
+// gather of every tile's slots into the packed list.  max_tiles bounds n_tiles.
+int launch_changed_lists(const CullView* views, const CullView& one, uint32_t n_views,
+                         uint32_t max_tiles, void* stream);
 
 // Transform propagation (xform.cu).
 struct XformLaunch {

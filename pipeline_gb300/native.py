@@ -57,6 +57,7 @@ _SIGS = {
     "dpcull_ctx_stream": (_P, [_P]),
     "dpcull_ctx_kernel_launches": (C.c_uint64, [_P]),
     "dpcull_ctx_device_bytes": (C.c_uint64, [_P]),
+    "dpcull_ctx_set_prefilter": (_I, [_P, _I]),
     "dpcull_group_create": (_I, [_P, _UP]),
     "dpcull_group_destroy": (_I, [_P, _U32]),
     "dpcull_group_set_objects": (_I, [_P, _U32, _SZ, _FP, _FP, _UP]),
@@ -75,6 +76,7 @@ _SIGS = {
     "dpcull_result_bits": (_I, [_P, _U32, _UP, _SZ, C.POINTER(_SZ)]),
     "dpcull_result_is_visible": (_I, [_P, _U32, _SZ, C.POINTER(_I)]),
     "dpcull_result_device": (_I, [_P, _U32, C.POINTER(_P), C.POINTER(_P), C.POINTER(_P)]),
+    "dpcull_result_move": (_I, [_P, _U32, _SZ, _SZ]),
     "dpcull_cull_batched": (_I, [_P, C.POINTER(Job), _SZ, C.POINTER(Tuning)]),
     "dpcull_plan_create": (_I, [_P, C.POINTER(Job), _SZ, C.POINTER(Tuning), _UP]),
     "dpcull_plan_set_views": (_I, [_P, _U32, _FP]),
@@ -180,6 +182,9 @@ class Context:
     @property
     def device_bytes(self) -> int:
         return int(self.lib.dpcull_ctx_device_bytes(self.h))
+
+    def set_prefilter(self, enabled: bool) -> None:
+        _check(self.lib.dpcull_ctx_set_prefilter(self.h, 1 if enabled else 0))
 
     # ---- groups ----
     def group_create(self) -> int:

@@ -332,6 +332,74 @@ def test_object_updates_and_appends(ctx):
     ctx.group_destroy(g)
 
 
+def near_plane_scene(seed: int, n: int, vp: np.ndarray):
+    """Tiny boxes centred on the frustum's boundary planes of `vp` (and on the extended
+    planes outside it), the worst case for the prefilter's error margins."""
+    rng = np.random.default_rng(seed)
+    M = np.asarray(vp, np.float64).reshape(4, 4)
+    Minv = np.linalg.inv(M)
+    ndc = rng.uniform(-1.3, 1.3, (n, 3))
+    axis = rng.integers(0, 3, n)
+    side = rng.choice([-1.0, 1.0], n)
+    ndc[np.arange(n), axis] = side * (1.0 + rng.choice([0.0, 1e-7, -1e-7, 1e-5, -1e-5, 1e-3], n))
+    w = rng.uniform(0.2, 3000.0, n)
+    clip = np.c_[ndc * w[:, None], w]
+    world = clip @ Minv
+    world = world[:, :3] / world[:, 3:4]
+    size = 10.0 ** rng.uniform(-6, 0.5, (3, n))
+    lower = (world.T - size / 2).astype(np.float32)
+    upper = (world.T + size / 2).astype(np.float32)
+    ident = np.eye(4, dtype=np.float32).reshape(1, 16)
+    mats = np.repeat(ident, 4, axis=0)
+    mats[1, 12:15] = [1e-3, 0, 0]
+    mats[2, :3] = [0.999999, 1e-4, 0]
+    mats[3, 3] = 1e-6  # projective
+    xform = rng.integers(0, 4, n, dtype=np.uint32)
+    return lower, upper, xform, mats
+
+
+@pytest.mark.parametrize("prefilter", [True, False])
+def test_prefilter_is_exact_near_planes(ctx, prefilter):
+    views = W.f32([W.perspective(), W.cube_face_views()[0], W.cascade_views()[1],
+                   W.stereo_views()[1], W.perspective(90.0, 1.0, 0.5, 100.0)])
+    for s, vp in enumerate(views):
+        lower, upper, xform, mats = near_plane_scene(50 + s, 40_000, vp)
+        lo, ex = box3_lower_extent(lower, upper)
+        g = ctx.group_create()
+        ctx.group_set_objects(g, lo, ex, xform)
+        ctx.group_set_matrices(g, mats)
+        ctx.set_prefilter(prefilter)
+        rs = [ctx.result_create(g) for _ in range(len(views))]
+        ctx.cull_batched([(g, rs, views)], dict(views_per_pass=8, tiles_per_ticket=1, ctas_per_sm=0))
+        r1 = ctx.result_create(g)
+        ctx.cull(g, r1, vp)
+        ctx.set_prefilter(True)
+        exp = oracle.cull_bits(lo, ex, xform, mats, vp)
+        assert np.array_equal(ctx.result_bits(r1), exp), (s, prefilter)
+        for r, v2 in zip(rs, views):
+            assert np.array_equal(ctx.result_bits(r), oracle.cull_bits(lo, ex, xform, mats, v2)), (s, prefilter)
+        ctx.group_destroy(g)
+
+
+def test_prefilter_equals_exact_on_golden_specials(ctx):
+    z = load_golden("scene_specials.npz")
+    lo, ex = box3_lower_extent(z["lower"], z["upper"])
+    g = ctx.group_create()
+    ctx.group_set_objects(g, lo, ex, z["xform"])
+    ctx.group_set_matrices(g, z["mats"])
+    out = {}
+    for pf in (True, False):
+        ctx.set_prefilter(pf)
+        rs = [ctx.result_create(g) for _ in z["vps"]]
+        ctx.cull_batched([(g, rs, z["vps"])])
+        out[pf] = [ctx.result_bits(r) for r in rs]
+    ctx.set_prefilter(True)
+    for a, b, k in zip(out[True], out[False], range(len(z["vps"]))):
+        assert np.array_equal(a, b)
+        assert np.array_equal(a, z[f"bits{k}"])  # visibility depends on the view only
+    ctx.group_destroy(g)
+
+
 def test_kernel_launch_counter(ctx):
     sc = W.plain_scene(5, 5000)
     g = setup_group(ctx, sc["lower"], sc["upper"], sc["xform"], sc["mats"])
