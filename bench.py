@@ -186,6 +186,8 @@ def run_ours(args, dist: Dist) -> dict | None:
     torch.cuda.set_device(device)
     wl = Stress(seed=3 + 1000 * dist.rank, n=args.objects, t=args.transforms)
     ctx = native.Context(device)
+    if args.exact_only:
+        ctx.set_prefilter(False)
     wl.setup(ctx, parse_tuning(args.tuning))
     tuning = ctx.plan_tuning(wl.plan)
     rng = np.random.default_rng(17 + dist.rank)
@@ -398,6 +400,8 @@ def main():
     ap.add_argument("--objects", type=int, default=STRESS_N, help="objects per GPU (smaller cases for profiling)")
     ap.add_argument("--transforms", type=int, default=STRESS_T)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--exact-only", action="store_true",
+                    help="disable the conservative prefilter (ablation; results are identical)")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     dist = Dist(args.gpus)

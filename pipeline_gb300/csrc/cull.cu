@@ -51,7 +51,7 @@ __device__ __forceinline__ uint32_t compu(const uint4& v, int k)
 
 struct CullShared {
   float vp[kMaxViewsPerPass][16];
-  float4 vn[kMaxViewsPerPass];                       // prefilter view bounds
+  PfView vn[kMaxViewsPerPass];                       // prefilter view bounds
   uint32_t vis[kMaxViewsPerPass][kTileWords];        // visibility from the exact drain
   uint32_t wtot[kMaxViewsPerPass][kThreads / 32];   // per-warp changed counts
   uint32_t item;
@@ -125,32 +125,56 @@ __device__ void process_item(const CullLaunch& a, uint32_t item, CullShared& sh)
   for (int v = 0; v < VPP; ++v) nib[v] = 0;
   uint32_t amb = 0;  // bit 8k + v: object k in view v needs the exact test
 
+  if (PF) {
+    // Boxes and their bounds for the 4 objects first (the 16 matrix gathers overlap),
+    // then each view's constants are read once for all 4 objects.
+    PfObject pb[kObjPerThread];
+    uint32_t valid = 0;
 #pragma unroll
-  for (int k = 0; k < kObjPerThread; ++k) {
-    if (obj0 + k < sc.n_objects) {
-      const uint32_t mi = compu(xf, k);
-      if (mi < sc.n_mats) {
-        const float4* M = mats + 4 * (size_t)mi;
-        const float4 r0 = __ldg(M + 0), r1 = __ldg(M + 1), r2 = __ldg(M + 2), r3 = __ldg(M + 3);
-        const Obb o = make_obb(comp(lx, k), comp(ly, k), comp(lz, k), comp(ex, k), comp(ey, k),
-                               comp(ez, k), r0, r1, r2, r3);
-        if (PF) {
-          const PfObject b = pf_object(o);
+    for (int k = 0; k < kObjPerThread; ++k) {
+      pb[k].da = pf_nan();
+      if (obj0 + k < sc.n_objects) {
+        const uint32_t mi = compu(xf, k);
+        if (mi < sc.n_mats) {
+          const float4* M = mats + 4 * (size_t)mi;
+          const Obb o = make_obb(comp(lx, k), comp(ly, k), comp(lz, k), comp(ex, k), comp(ey, k),
+                                 comp(ez, k), __ldg(M + 0), __ldg(M + 1), __ldg(M + 2), __ldg(M + 3));
+          pb[k] = pf_object(o);
+          valid |= 1u << k;
+        } else if (atomicOr(&a.ctl->error, kErrBadTransform) == 0) {
+          a.ctl->error_info = obj0 + k;
+        }
+      }
+    }
 #pragma unroll
-          for (int v = 0; v < VPP; ++v) {
-            if (v < nv) {
-              const int cls = pf_classify(b, sh.vp[v], sh.vn[v]);
-              if (cls == kPfVisible) nib[v] |= 1u << k;
-              else if (cls == kPfAmbiguous) amb |= 1u << (8 * k + v);
-            }
+    for (int v = 0; v < VPP; ++v) {
+      if (v < nv) {
+        const PfViewRegs vr = pf_load_view(sh.vp[v], sh.vn[v]);
+#pragma unroll
+        for (int k = 0; k < kObjPerThread; ++k) {
+          if (valid & (1u << k)) {
+            const int cls = pf_classify(pb[k], vr);
+            if (cls == kPfVisible) nib[v] |= 1u << k;
+            else if (cls == kPfAmbiguous) amb |= 1u << (8 * k + v);
           }
-        } else {
+        }
+      }
+    }
+  } else {
+#pragma unroll
+    for (int k = 0; k < kObjPerThread; ++k) {
+      if (obj0 + k < sc.n_objects) {
+        const uint32_t mi = compu(xf, k);
+        if (mi < sc.n_mats) {
+          const float4* M = mats + 4 * (size_t)mi;
+          const Obb o = make_obb(comp(lx, k), comp(ly, k), comp(lz, k), comp(ex, k), comp(ey, k),
+                                 comp(ez, k), __ldg(M + 0), __ldg(M + 1), __ldg(M + 2), __ldg(M + 3));
 #pragma unroll
           for (int v = 0; v < VPP; ++v)
             if (v < nv && obb_visible(o, sh.vp[v])) nib[v] |= 1u << k;
+        } else if (atomicOr(&a.ctl->error, kErrBadTransform) == 0) {
+          a.ctl->error_info = obj0 + k;
         }
-      } else {
-        if (atomicOr(&a.ctl->error, kErrBadTransform) == 0) a.ctl->error_info = obj0 + k;
       }
     }
   }
@@ -259,7 +283,7 @@ __device__ void process_item(const CullLaunch& a, uint32_t item, CullShared& sh)
 }
 
 template <int VPP, bool PF>
-__global__ void __launch_bounds__(kThreads) cull_kernel(const __grid_constant__ CullLaunch a)
+__global__ void __launch_bounds__(kThreads, 3) cull_kernel(const __grid_constant__ CullLaunch a)
 {
   __shared__ CullShared sh;
   CullControl* ctl = a.ctl;
