@@ -204,6 +204,36 @@ int dpcull_tree_world(dpcull_ctx ctx, dpcull_tree t, size_t first, size_t count,
 /* Dirty-world bits of the last compute (the EventWorldMatricesChanged payload). */
 int dpcull_tree_dirty_world(dpcull_ctx ctx, dpcull_tree t, uint32_t* words, size_t n_words);
 
+/* ---- cull without allocation -------------------------------------------------------
+ * No counterpart in the reference: an extra entry point of this library for callers
+ * that cannot allocate device memory when they cull -- a frame loop that must not hit
+ * cudaMalloc's implicit device synchronisation, or a process whose device memory is all
+ * owned by another allocator (a framework's caching allocator, a budget reserved up
+ * front).  It runs the plain cull of dpcull_cull on buffers the caller owns and takes its
+ * scratch from one static device array of about 4 MB that every GPU loading this
+ * library holds until the process exits; it calls no cudaMalloc, cudaFree or other
+ * allocating routine.
+ *   objects   device, 16-byte aligned: 7 rows of `cap` entries -- lower x, y, z,
+ *             extent x, y, z (float) and the transform index (uint32);
+ *             cap is a multiple of 1024 and >= n; n <= DPCULL_NOALLOC_MAX_OBJECTS
+ *             (larger n: DPCULL_ERR_CAPACITY)
+ *   matrices  device, 16-byte aligned, n_matrices x 16 floats
+ *   bits      device, cap/32 words: the previous visibility on entry (a result that was
+ *             never culled is all ones for objects 0..n-1, zero past n), the new
+ *             visibility on return
+ *   changed   device, n entries: the ascending list of objects whose bit changed;
+ *   n_changed device, one word: its length
+ * The first call on a device looks up the scratch array's address with that device
+ * current; make it before any stream capture.  Every call shares the array (it keeps the
+ * last call's contents; each call clears what must start at zero), so calls whose work
+ * overlaps on the GPU race.  Returns after the work on `stream` has finished;
+ * DPCULL_ERR_OUT_OF_RANGE if a transform index is past the matrix array (those objects
+ * are left invisible). */
+#define DPCULL_NOALLOC_MAX_OBJECTS (1u << 20)
+int dpcull_cull_noalloc(const float* objects, size_t cap, size_t n, const float* matrices,
+                        size_t n_matrices, const float vp[16], uint32_t* bits, uint32_t* changed,
+                        uint32_t* n_changed, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -523,6 +523,8 @@ void tune_cache_store(const std::string& key, const dpcull_tuning& t)
 
 }  // namespace
 
+int dpcull::record_error(int code, const char* msg) { return fail(code, "%s", msg); }
+
 // ===================================================================================
 extern "C" {
 

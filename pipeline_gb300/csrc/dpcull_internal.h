@@ -99,6 +99,9 @@ int launch_scatter_matrices(float* dst, const float* src, const uint32_t* idx, u
 int launch_scatter_objects(float* soa, uint32_t cap, const float* src, const uint32_t* idx,
                            uint32_t k, void* stream);
 
+// Sets the calling thread's dpcull_last_error() message; returns code (api.cu).
+int record_error(int code, const char* msg);
+
 // Bounding box (bbox.cu): partials has room for bbox_partials_needed() floats.
 size_t bbox_partials_needed(uint32_t n_objects);
 int launch_bbox(const float* soa, uint32_t cap, uint32_t n, const float* mats, float* partials,

@@ -94,7 +94,10 @@ _SIGS = {
     "dpcull_tree_world_device": (_I, [_P, _U32, C.POINTER(_P), C.POINTER(_SZ)]),
     "dpcull_tree_world": (_I, [_P, _U32, _SZ, _SZ, _FP]),
     "dpcull_tree_dirty_world": (_I, [_P, _U32, _UP, _SZ]),
+    "dpcull_cull_noalloc": (_I, [_P, _SZ, _SZ, _P, _SZ, _FP, _P, _P, _P, _P]),
 }
+
+NOALLOC_MAX_OBJECTS = 1 << 20  # DPCULL_NOALLOC_MAX_OBJECTS
 
 _lib = None
 
