@@ -245,6 +245,12 @@ def run_ours(args, dist: Dist) -> dict | None:
     # -- end to end through the C ABI with host buffers --
     e2e = run_e2e(ctx, wl, frames, args, dist)
 
+    # -- serving loop (device-resident catalogue, continuous batching) --
+    serving_res = None
+    if args.serve_seconds > 0 and dist.rank == 0:
+        ctx.group_destroy(wl.g)  # free the stress scene before filling the budget
+        serving_res = run_serving(ctx, args)
+
     bytes_launch = wl.algorithmic_bytes(sum(changed))
     pk = peaks()
     achieved = bytes_launch / (ms_step / 1e3) / 1e9
@@ -268,7 +274,7 @@ def run_ours(args, dist: Dist) -> dict | None:
                      "peak_source": pk["source"], "algorithmic_bytes_per_launch": bytes_launch,
                      "kernel": "cull_kernel (persistent, graph replay; event time per step)"},
         "e2e": e2e, "gpu_launches": launches, "clocks": clk, "parity_sample": parity,
-        "changed_per_step": changed,
+        "changed_per_step": changed, "serving": serving_res,
     }
     ctx.close()
     return out
@@ -324,6 +330,35 @@ def traffic_from_profile(wl) -> int | None:
     d = json.loads(p.read_text())
     scale = (wl.n * wl.v) / (d["objects"] * d["views"])
     return int(d["dram_bytes_per_launch"] * scale)
+
+
+# ---- serving (config 4) ----------------------------------------------------------------------------
+def run_serving(ctx, args) -> dict:
+    """64 Poisson clients (mean args.serve_rate requests/s) against a catalogue whose
+    resident bytes exceed the HBM budget (LRU eviction runs); p50/p99 latency from the
+    scheduled arrival to the completion seen by the server."""
+    from pipeline_gb300 import native, serving
+
+    budget = int(args.serve_budget_gb * 1e9)
+    templates = serving.make_templates(seed=4, n_templates=args.serve_templates)
+    avg = float(np.mean([serving.scene_bytes(t["n"], t["mats"].shape[0]) for t in templates]))
+    n_scenes = int(math.ceil(1.25 * budget / avg))
+    times, scenes, nviews, vps = serving.schedule(seed=44, n_scenes=n_scenes,
+                                                  duration_s=args.serve_seconds, rate=args.serve_rate)
+    with native.Server(ctx, budget, n_streams=3, max_batch_objects=48 << 20) as srv:
+        for k in range(n_scenes):
+            t = templates[k % len(templates)]
+            srv.add_scene(k, t["lower"], t["extent"], t["xform"], t["mats"])
+        res = serving.run_load(srv, times, scenes, nviews, vps, warmup_s=args.serve_warmup)
+        st = srv.stats()
+    res.update({"budget_gb": budget / 1e9, "catalogue_scenes": n_scenes,
+                "catalogue_gb": n_scenes * avg / 1e9, "templates": len(templates),
+                "clients": 64, "rate_req_per_s": args.serve_rate, "seconds": args.serve_seconds,
+                "warmup_s": args.serve_warmup, "evictions": st["scene_evictions"],
+                "uploads": st["scene_uploads"], "upload_gb": st["upload_bytes"] / 1e9,
+                "batches": st["batches"], "max_batch_requests": st["max_batch_requests"],
+                "streams": 3})
+    return res
 
 
 # ---- CPU baseline (oracle port on the host cores) ----------------------------------------------
@@ -394,12 +429,17 @@ def main():
     ap.add_argument("--steps", type=int, default=400)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--workload", default="stress", choices=["stress"])
+    ap.add_argument("--workload", default="stress", choices=["stress", "serving"])
     ap.add_argument("--tuning", default=None, help="JSON tuning (default: autotuner)")
     ap.add_argument("--cpu-sample", type=int, default=1_000_000)
     ap.add_argument("--objects", type=int, default=STRESS_N, help="objects per GPU (smaller cases for profiling)")
     ap.add_argument("--transforms", type=int, default=STRESS_T)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--serve-seconds", type=float, default=5.0, help="serving run length (0 = skip)")
+    ap.add_argument("--serve-warmup", type=float, default=1.0)
+    ap.add_argument("--serve-rate", type=float, default=20_000.0)
+    ap.add_argument("--serve-budget-gb", type=float, default=150.0)
+    ap.add_argument("--serve-templates", type=int, default=32)
     ap.add_argument("--exact-only", action="store_true",
                     help="disable the conservative prefilter (ablation; results are identical)")
     args = ap.parse_args()
@@ -407,6 +447,14 @@ def main():
     dist = Dist(args.gpus)
     if args.impl == "reference":
         out = run_reference(args, dist)
+    elif args.workload == "serving":
+        from pipeline_gb300 import build, native
+
+        build.build_all()
+        ctx = native.Context(dist.local)
+        out = {"metric": "serving: p50/p99 request latency and culled object-views/s", "workload": "serving",
+               "serving": run_serving(ctx, args)}
+        ctx.close()
     else:
         out = run_ours(args, dist)
         if out is not None and dist.rank == 0 and not args.no_cpu_baseline:

@@ -204,6 +204,68 @@ int dpcull_tree_world(dpcull_ctx ctx, dpcull_tree t, size_t first, size_t count,
 /* Dirty-world bits of the last compute (the EventWorldMatricesChanged payload). */
 int dpcull_tree_dirty_world(dpcull_ctx ctx, dpcull_tree t, uint32_t* words, size_t n_words);
 
+/* ---- serving: device-resident scenes, continuous batching ---------------------------
+ * A server keeps a pool of scenes resident in HBM under a byte budget (least recently
+ * used scenes with no work in flight are evicted when a request needs room), admits cull
+ * requests as they arrive, and packs every admissible pending request into the next
+ * batch as soon as one of its streams is free: each batch is one persistent launch over
+ * all (scene, view) pairs of its requests, batches on different streams overlap on the
+ * device, and uploads of newly admitted scenes run on the batch's stream.  A request
+ * culls one scene under 1..8 view-projections; its result is the visibility words of each
+ * view (and the visible count), exactly those of dpcull_cull on the same data.  The
+ * serving loop of the reference renderer has no counterpart: this is the GB300 service
+ * around the cull of dp/culling/cpu/src/ManagerImpl.cpp:467-518. */
+typedef struct dpcull_server_s* dpcull_server;
+
+#define DPCULL_SERVER_MAX_VIEWS 8
+#define DPCULL_REQUEST_KEEP_BITS 1u /* keep the visibility words for dpcull_server_result */
+
+typedef struct dpcull_completion {
+  uint64_t request;
+  uint32_t scene;
+  uint32_t n_views;
+  uint32_t visible[DPCULL_SERVER_MAX_VIEWS]; /* visible objects per view */
+  uint64_t objects;                          /* objects of the scene */
+  double submit_s, start_s, done_s;          /* dpcull_server_now() clock */
+  int32_t status;                            /* DPCULL_OK or an error code */
+  uint32_t pad;
+} dpcull_completion;
+
+typedef struct dpcull_server_stats {
+  uint64_t requests_submitted, requests_completed, batches;
+  uint64_t scene_uploads, scene_evictions, upload_bytes;
+  uint64_t resident_bytes, resident_scenes, budget_bytes;
+  uint64_t max_batch_requests, pending_requests;
+} dpcull_server_stats;
+
+/* Steady-clock seconds; the clock of dpcull_completion's timestamps. */
+double dpcull_server_now(void);
+/* n_streams batches may be in flight at once (1..8); max_batch_objects caps the
+ * object-views of one batch (latency bound); the scheduler runs on its own thread. */
+int dpcull_server_create(dpcull_ctx ctx, uint64_t budget_bytes, uint32_t n_streams,
+                         uint64_t max_batch_objects, dpcull_server* out);
+int dpcull_server_destroy(dpcull_server s);
+/* Registers scene `scene` (ids are dense small integers).  The host arrays are copied
+ * now into a pinned staging buffer in the device layout (scenes registered with the same
+ * arrays share it), so every later upload is one asynchronous copy; the caller may free
+ * them afterwards.  Planar lower[3][n] / extent[3][n], uint32 xform[n], n_matrices x 16
+ * floats. */
+int dpcull_server_add_scene(dpcull_server s, uint32_t scene, size_t n, const float* lower,
+                            const float* extent, const uint32_t* xform, const float* matrices,
+                            size_t n_matrices);
+/* Thread-safe.  vps: n_views x 16 floats (copied). */
+int dpcull_server_submit(dpcull_server s, uint32_t scene, uint32_t n_views, const float* vps,
+                         uint32_t flags, uint64_t* request);
+/* Completed requests since the last poll (up to cap); *n receives the count. */
+int dpcull_server_poll(dpcull_server s, dpcull_completion* out, size_t cap, size_t* n);
+/* Visibility words of view `view` of a completed DPCULL_REQUEST_KEEP_BITS request. */
+int dpcull_server_result(dpcull_server s, uint64_t request, uint32_t view, uint32_t* words,
+                         size_t n_words);
+int dpcull_server_release(dpcull_server s, uint64_t request);
+/* Waits until every submitted request has completed. */
+int dpcull_server_drain(dpcull_server s);
+int dpcull_server_get_stats(dpcull_server s, dpcull_server_stats* out);
+
 /* ---- cull without allocation -------------------------------------------------------
  * No counterpart in the reference: an extra entry point of this library for callers
  * that cannot allocate device memory when they cull -- a frame loop that must not hit

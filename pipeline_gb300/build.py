@@ -26,7 +26,7 @@ LIB = PKG / "_lib"
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-lineinfo", "--fmad=false", "-ftz=false", "-prec-div=true",
               "-prec-sqrt=true", "-std=c++17", "-Xcompiler", "-fPIC", "-I", str(ROOT / "include")]
-CU_SOURCES = ["api.cu", "cull.cu", "xform.cu", "bbox.cu", "noalloc.cu"]
+CU_SOURCES = ["api.cu", "cull.cu", "xform.cu", "bbox.cu", "noalloc.cu", "serve.cu"]
 
 
 def nvcc() -> str:

@@ -525,6 +525,12 @@ void tune_cache_store(const std::string& key, const dpcull_tuning& t)
 
 int dpcull::record_error(int code, const char* msg) { return fail(code, "%s", msg); }
 
+void dpcull::ctx_info(dpcull_ctx_s* c, int* device, int* sm_count)
+{
+  *device = c->device;
+  *sm_count = c->sm_count;
+}
+
 // ===================================================================================
 extern "C" {
 

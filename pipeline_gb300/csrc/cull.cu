@@ -224,14 +224,21 @@ __device__ void process_item(const CullLaunch& a, uint32_t item, CullShared& sh)
     chg[v] = 0;
     if (v < nv) {  // nv is uniform over the CTA, so the shuffles stay warp-uniform
       uint32_t* bits = views[v].bits;
-      const uint32_t prev = bits[word];
-      chg[v] = nib[v] ^ ((prev >> shift) & 0xFu);
+      const bool track = !(views[v].flags & kViewNoChanged);
+      const uint32_t prev = track ? bits[word] : ~0u;
       uint32_t w = nib[v] << shift;
       w |= __shfl_xor_sync(0xffffffffu, w, 1);
       w |= __shfl_xor_sync(0xffffffffu, w, 2);
       w |= __shfl_xor_sync(0xffffffffu, w, 4);
-      if ((tid & 7) == 0 && w != prev) bits[word] = w;
-      packed[v >> 2] |= (uint32_t)__popc(chg[v]) << (8 * (v & 3));
+      if ((tid & 7) == 0 && (!track || w != prev)) bits[word] = w;
+      if (views[v].n_visible) {
+        const uint32_t cnt = __reduce_add_sync(0xffffffffu, (uint32_t)__popc(nib[v]));
+        if (lane == 0 && cnt) atomicAdd(views[v].n_visible, cnt);
+      }
+      if (track) {
+        chg[v] = nib[v] ^ ((prev >> shift) & 0xFu);
+        packed[v >> 2] |= (uint32_t)__popc(chg[v]) << (8 * (v & 3));
+      }
     }
   }
 
@@ -257,7 +264,7 @@ __device__ void process_item(const CullLaunch& a, uint32_t item, CullShared& sh)
   // ---- the tile's changed objects, ascending, into its private slots ----
 #pragma unroll
   for (int v = 0; v < VPP; ++v) {
-    if (v < nv) {
+    if (v < nv && !(views[v].flags & kViewNoChanged)) {
       uint32_t before = 0, total = 0;
 #pragma unroll
       for (int w = 0; w < kThreads / 32; ++w) {
@@ -319,8 +326,15 @@ __global__ void __launch_bounds__(kScanThreads)
   const uint32_t n = v.n_tiles;
   const uint32_t per = (n + kScanThreads - 1) / kScanThreads;
   const uint32_t b = min(n, threadIdx.x * per), e = min(n, b + per);
+  // Independent loads, 8 in flight per thread (the counts were just written by the cull).
   uint32_t s = 0;
-  for (uint32_t i = b; i < e; ++i) s += v.counts[i];
+  for (uint32_t i = b; i < e; i += 8) {
+    uint32_t c[8];
+#pragma unroll
+    for (int j = 0; j < 8; ++j) c[j] = i + j < e ? __ldcg(v.counts + i + j) : 0u;
+#pragma unroll
+    for (int j = 0; j < 8; ++j) s += c[j];
+  }
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   uint32_t x = s;
 #pragma unroll
@@ -341,26 +355,41 @@ __global__ void __launch_bounds__(kScanThreads)
   }
   __syncthreads();
   uint32_t run = (warp ? warp_sum[warp - 1] : 0u) + x - s;
-  for (uint32_t i = b; i < e; ++i) {
-    const uint32_t c = v.counts[i];
-    v.offsets[i] = run;
-    run += c;
+  for (uint32_t i = b; i < e; i += 8) {
+    uint32_t c[8];
+#pragma unroll
+    for (int j = 0; j < 8; ++j) c[j] = i + j < e ? __ldcg(v.counts + i + j) : 0u;
+#pragma unroll
+    for (int j = 0; j < 8; ++j)
+      if (i + j < e) {
+        v.offsets[i + j] = run;
+        run += c[j];
+      }
   }
   if (threadIdx.x == kScanThreads - 1) *v.n_changed = warp_sum[31];
 }
 
-// blockIdx.y = view; each warp copies whole tiles' slot ranges to their packed position.
+// blockIdx.y = view.  Each warp reads the counts and offsets of 32 consecutive tiles in
+// one coalesced load, then copies the slot ranges of the non-empty ones, all lanes per
+// tile, to their packed positions.
 __global__ void gather_changed_kernel(const CullView* views, const __grid_constant__ CullView one)
 {
   const CullView& v = views ? views[blockIdx.y] : one;
   const int lane = threadIdx.x & 31;
   const uint32_t warps = blockDim.x / 32;
-  for (uint32_t t = blockIdx.x * warps + threadIdx.x / 32; t < v.n_tiles; t += gridDim.x * warps) {
-    const uint32_t c = v.counts[t];
-    if (!c) continue;
-    const uint32_t o = v.offsets[t];
-    const uint32_t* src = v.slots + (size_t)t * kTileObjects;
-    for (uint32_t j = lane; j < c; j += 32) v.changed[o + j] = src[j];
+  for (uint32_t t0 = (blockIdx.x * warps + threadIdx.x / 32) * 32; t0 < v.n_tiles;
+       t0 += gridDim.x * warps * 32) {
+    const uint32_t t = t0 + lane;
+    const uint32_t c = t < v.n_tiles ? __ldcg(v.counts + t) : 0u;
+    const uint32_t o = t < v.n_tiles ? __ldcg(v.offsets + t) : 0u;
+    uint32_t busy = __ballot_sync(0xffffffffu, c != 0);
+    while (busy) {
+      const int k = __ffs(busy) - 1;
+      busy &= busy - 1u;
+      const uint32_t ck = __shfl_sync(0xffffffffu, c, k), ok = __shfl_sync(0xffffffffu, o, k);
+      const uint32_t* src = v.slots + (size_t)(t0 + k) * kTileObjects;
+      for (uint32_t j = lane; j < ck; j += 32) v.changed[ok + j] = __ldcg(src + j);
+    }
   }
 }
 
@@ -432,9 +461,9 @@ int launch_changed_lists(const CullView* views, const CullView& one, uint32_t n_
   cudaStream_t s = static_cast<cudaStream_t>(stream);
   if (!n_views) return 0;
   scan_counts_kernel<<<n_views, kScanThreads, 0, s>>>(views, one);
-  const uint32_t warps = 8;
-  uint32_t gx = (max_tiles + warps - 1) / warps;
-  if (gx > 64) gx = 64;
+  const uint32_t warps = 8, tiles_per_cta = warps * 32;
+  uint32_t gx = (max_tiles + tiles_per_cta - 1) / tiles_per_cta;
+  if (gx > 1024) gx = 1024;
   if (gx < 1) gx = 1;
   gather_changed_kernel<<<dim3(gx, n_views), warps * 32, 0, s>>>(views, one);
   return cudaGetLastError() == cudaSuccess ? 0 : -1;

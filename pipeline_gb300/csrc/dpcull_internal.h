@@ -16,6 +16,8 @@
 #include <cstddef>
 #include <cstdint>
 
+struct dpcull_ctx_s;
+
 namespace dpcull {
 
 constexpr int kThreads = 256;                      // threads per CTA
@@ -50,8 +52,13 @@ struct CullView {
   uint32_t* counts;      // scratch: changed objects per tile
   uint32_t* offsets;     // scratch: exclusive prefix of counts
   uint32_t n_tiles;
-  uint32_t pad;
+  uint32_t flags;        // kViewNoChanged: write the visibility words only
+  uint32_t* n_visible;   // optional: number of visible objects (accumulated)
 };
+
+// CullView::flags: no previous visibility and no changed list (bits are overwritten;
+// changed / n_changed / slots / counts / offsets are not used).
+constexpr uint32_t kViewNoChanged = 1u;
 
 struct CullControl {
   unsigned int ticket;     // next work item
@@ -101,6 +108,8 @@ int launch_scatter_objects(float* soa, uint32_t cap, const float* src, const uin
 
 // Sets the calling thread's dpcull_last_error() message; returns code (api.cu).
 int record_error(int code, const char* msg);
+// CUDA ordinal and SM count of a context (api.cu).
+void ctx_info(::dpcull_ctx_s* ctx, int* device, int* sm_count);
 
 // Bounding box (bbox.cu): partials has room for bbox_partials_needed() floats.
 size_t bbox_partials_needed(uint32_t n_objects);

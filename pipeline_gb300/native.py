@@ -95,7 +95,37 @@ _SIGS = {
     "dpcull_tree_world": (_I, [_P, _U32, _SZ, _SZ, _FP]),
     "dpcull_tree_dirty_world": (_I, [_P, _U32, _UP, _SZ]),
     "dpcull_cull_noalloc": (_I, [_P, _SZ, _SZ, _P, _SZ, _FP, _P, _P, _P, _P]),
+    "dpcull_server_now": (C.c_double, []),
+    "dpcull_server_create": (_I, [_P, C.c_uint64, _U32, C.c_uint64, C.POINTER(_P)]),
+    "dpcull_server_destroy": (_I, [_P]),
+    "dpcull_server_add_scene": (_I, [_P, _U32, _SZ, _FP, _FP, _UP, _FP, _SZ]),
+    "dpcull_server_submit": (_I, [_P, _U32, _U32, _FP, _U32, C.POINTER(C.c_uint64)]),
+    "dpcull_server_poll": (_I, [_P, _P, _SZ, C.POINTER(_SZ)]),
+    "dpcull_server_result": (_I, [_P, C.c_uint64, _U32, _UP, _SZ]),
+    "dpcull_server_release": (_I, [_P, C.c_uint64]),
+    "dpcull_server_drain": (_I, [_P]),
+    "dpcull_server_get_stats": (_I, [_P, _P]),
 }
+
+SERVER_MAX_VIEWS = 8
+REQUEST_KEEP_BITS = 1
+
+
+class Completion(C.Structure):
+    _fields_ = [("request", C.c_uint64), ("scene", _U32), ("n_views", _U32),
+                ("visible", _U32 * SERVER_MAX_VIEWS), ("objects", C.c_uint64),
+                ("submit_s", C.c_double), ("start_s", C.c_double), ("done_s", C.c_double),
+                ("status", C.c_int32), ("pad", _U32)]
+
+
+class ServerStats(C.Structure):
+    _fields_ = [(name, C.c_uint64) for name in (
+        "requests_submitted", "requests_completed", "batches", "scene_uploads", "scene_evictions",
+        "upload_bytes", "resident_bytes", "resident_scenes", "budget_bytes", "max_batch_requests",
+        "pending_requests")]
+
+    def as_dict(self) -> dict:
+        return {name: int(getattr(self, name)) for name, _ in self._fields_}
 
 NOALLOC_MAX_OBJECTS = 1 << 20  # DPCULL_NOALLOC_MAX_OBJECTS
 
@@ -375,3 +405,85 @@ class Context:
         out = np.zeros(n_words, np.uint32)
         _check(self.lib.dpcull_tree_dirty_world(self.h, t, uptr(out), n_words))
         return out
+
+
+class Server:
+    """A dpcull culling service (include/dpcull.h, serving section) on a context."""
+
+    def __init__(self, ctx: Context, budget_bytes: int, n_streams: int = 3,
+                 max_batch_objects: int = 32 << 20):
+        self.ctx = ctx
+        self.lib = ctx.lib
+        h = _P()
+        _check(self.lib.dpcull_server_create(ctx.h, int(budget_bytes), n_streams, int(max_batch_objects),
+                                             C.byref(h)))
+        self.h = h
+        self._scenes: dict = {}  # host arrays stay alive while the server lives
+        self._buf = (Completion * 4096)()
+
+    def close(self) -> None:
+        if self.h:
+            _check(self.lib.dpcull_server_destroy(self.h))
+            self.h = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def now(self) -> float:
+        return float(self.lib.dpcull_server_now())
+
+    def add_scene(self, scene: int, lower, extent, xform, mats) -> None:
+        lo, ex, xf, m = _f32(lower), _f32(extent), _u32(xform), _f32(mats).reshape(-1, 16)
+        self._scenes[scene] = (lo, ex, xf, m)
+        _check(self.lib.dpcull_server_add_scene(self.h, scene, xf.shape[0], fptr(lo), fptr(ex), uptr(xf),
+                                                fptr(m), m.shape[0]))
+
+    def submit(self, scene: int, vps, keep_bits: bool = False) -> int:
+        v = _f32(vps).reshape(-1)
+        rid = C.c_uint64()
+        _check(self.lib.dpcull_server_submit(self.h, scene, v.shape[0] // 16, fptr(v),
+                                             REQUEST_KEEP_BITS if keep_bits else 0, C.byref(rid)))
+        return rid.value
+
+    def submit_raw(self, scene: int, n_views: int, vps_ptr, rid) -> int:
+        """Low-overhead submit for load generators (pointer to n_views x 16 floats)."""
+        return self.lib.dpcull_server_submit(self.h, scene, n_views, vps_ptr, 0, rid)
+
+    def poll_array(self) -> np.ndarray:
+        """All completions so far as a numpy structured array (fast path)."""
+        parts = []
+        while True:
+            n = _SZ()
+            _check(self.lib.dpcull_server_poll(self.h, self._buf, len(self._buf), C.byref(n)))
+            if n.value:
+                parts.append(np.ctypeslib.as_array(self._buf)[: n.value].copy())
+            if n.value < len(self._buf):
+                break
+        if not parts:
+            return np.ctypeslib.as_array(self._buf)[:0].copy()
+        return np.concatenate(parts)
+
+    def poll(self) -> list:
+        a = self.poll_array()
+        return [(int(c["request"]), int(c["scene"]), int(c["n_views"]), list(c["visible"][: c["n_views"]]),
+                 int(c["objects"]), float(c["submit_s"]), float(c["start_s"]), float(c["done_s"]),
+                 int(c["status"])) for c in a]
+
+    def result(self, request: int, view: int, n_words: int) -> np.ndarray:
+        out = np.zeros(n_words, np.uint32)
+        _check(self.lib.dpcull_server_result(self.h, request, view, uptr(out), n_words))
+        return out
+
+    def release(self, request: int) -> None:
+        _check(self.lib.dpcull_server_release(self.h, request))
+
+    def drain(self) -> None:
+        _check(self.lib.dpcull_server_drain(self.h))
+
+    def stats(self) -> dict:
+        st = ServerStats()
+        _check(self.lib.dpcull_server_get_stats(self.h, C.byref(st)))
+        return st.as_dict()
