@@ -332,6 +332,169 @@ def traffic_from_profile(wl) -> int | None:
     return int(d["dram_bytes_per_launch"] * scale)
 
 
+# ---- other configurations (separate JSON lines; not the headline) ------------------------------
+def _events(torch, n):
+    return [torch.cuda.Event(enable_timing=True) for _ in range(n)]
+
+
+def run_plain_config(ctx, args) -> dict:
+    """Plain configuration: 100k objects with their own matrices, one view; a step is one
+    dpcull_cull plus the changed list and the visibility words read back (the reference's
+    cull call), alternating two frames 1 degree apart."""
+    import torch
+
+    sc = W.plain_scene(0, 100_000)
+    g = ctx.group_create()
+    ctx.group_set_objects(g, sc["lower"], sc["extent"], sc["xform"])
+    ctx.group_set_matrices(g, sc["mats"])
+    r = ctx.result_create(g)
+    bits = np.zeros(3125, np.uint32)
+    changed = np.zeros(100_000, np.uint32)
+    for i in range(args.warmup):
+        ctx.cull(g, r, sc["vps"][i % 2])
+        ctx.result_changed(r, changed)
+    lat = []
+    for i in range(args.steps):
+        t0 = time.perf_counter()
+        ctx.cull(g, r, sc["vps"][i % 2])
+        ctx.result_changed(r, changed)
+        ctx.result_bits(r, bits)
+        lat.append(time.perf_counter() - t0)
+    stream = torch.cuda.ExternalStream(ctx.stream)
+    ev = _events(torch, 2)
+    with torch.cuda.stream(stream):
+        ev[0].record(stream)
+        for i in range(args.steps):
+            ctx.cull(g, r, sc["vps"][i % 2])
+        ev[1].record(stream)
+    ctx.synchronize()
+    dev_ms = ev[0].elapsed_time(ev[1]) / args.steps
+    lat = np.asarray(lat) * 1e3
+    import oracle
+
+    obbs = oracle.build_obbs(sc["lower"], sc["extent"], sc["xform"], sc["mats"])
+    prev = np.zeros(3125, np.uint32)
+    ts = []
+    for i in range(9):
+        t0 = time.perf_counter()
+        b = oracle.cull_obbs(obbs, sc["vps"][i % 2])
+        oracle.update_changed(prev, b, 100_000)
+        ts.append(time.perf_counter() - t0)
+    cpu_ms = sorted(ts)[4] * 1e3
+    ctx.group_destroy(g)
+    return {"workload": "plain: 100k objects, own matrices, 1 view, 2 frames 1 deg apart",
+            "device_ms_per_cull": dev_ms, "object_views_per_s_device": 100_000 / (dev_ms / 1e3),
+            "e2e_p50_ms": float(np.percentile(lat, 50)), "e2e_p99_ms": float(np.percentile(lat, 99)),
+            "object_views_per_s_e2e": 100_000 / (np.median(lat) / 1e3),
+            "cpu_port_1core_ms": cpu_ms, "cpu_object_views_per_s": 100_000 / (cpu_ms / 1e3)}
+
+
+def run_hierarchy_config(ctx, args) -> dict:
+    """Hierarchy configuration: 4M objects over 64k transforms of a depth-8 tree; every
+    frame uploads all local matrices (animated), propagates them on the GPU and culls
+    through the device world matrices under the next camera of a radius-800 orbit."""
+    import torch
+
+    from pipeline_gb300.transform import Tree
+
+    sc = W.hierarchy_scene(seed=1, frames=240)
+    used = sc["n_transforms"]
+    t = Tree(ctx)
+    for p, x in sc["pairs"]:
+        t.add_transform(int(p), sc["locals"][x])
+    t.compute()
+    dev, count = t.world_device()
+    g = ctx.group_create()
+    ctx.group_set_objects(g, sc["lower"], sc["extent"], sc["xform"])
+    ctx.group_bind_device_matrices(g, dev, count)
+    r = ctx.result_create(g)
+    idx = np.arange(1, used, dtype=np.uint32)
+    locs = np.ascontiguousarray(sc["locals"][1:])
+    stream = torch.cuda.ExternalStream(ctx.stream)
+    frames = sc["vps"].shape[0]
+    for i in range(args.warmup):
+        ctx.tree_set_locals(t.handle, idx, locs)
+        ctx.tree_compute(t.handle)
+        ctx.cull(g, r, sc["vps"][i % frames])
+    ctx.synchronize()
+    ev = _events(torch, 4)
+    n = min(args.steps, frames)
+    up_ms = prop_ms = cull_ms = 0.0
+    t0 = time.perf_counter()
+    for i in range(n):
+        with torch.cuda.stream(stream):
+            ev[0].record(stream)
+            u0 = time.perf_counter()
+            ctx.tree_set_locals(t.handle, idx, locs)  # host staging + H2D + scatter (dirty bits)
+            up_ms += (time.perf_counter() - u0) * 1e3
+            ev[1].record(stream)
+            ctx.tree_compute(t.handle)
+            ev[2].record(stream)
+            ctx.cull(g, r, sc["vps"][i % frames])
+            ev[3].record(stream)
+        ch = ctx.result_changed(r)
+        prop_ms += ev[1].elapsed_time(ev[2])
+        cull_ms += ev[2].elapsed_time(ev[3])
+    wall_ms = (time.perf_counter() - t0) * 1e3 / n
+    ctx.group_destroy(g)
+    return {"workload": f"hierarchy: 4M objects, {used} transforms (depth 8, branching 2-8), orbit r=800",
+            "frames": n, "ms_per_frame_e2e": wall_ms, "upload_locals_host_ms": up_ms / n,
+            "propagate_ms": prop_ms / n, "cull_ms": cull_ms / n,
+            "propagate_transforms_per_s": (used - 1) / (prop_ms / n / 1e3),
+            "object_views_per_s_e2e": 4_000_000 / (wall_ms / 1e3),
+            "note": "per frame: all 64k local matrices updated from host memory (4 MB), GPU propagation, "
+                    "cull through the device world matrices, changed list read back"}
+
+
+def run_batched_config(ctx, args) -> dict:
+    """Batched-uneven configuration: 256 scenes of 1k-1M objects (log-uniform) with 1-6
+    views each; one captured persistent plan vs one plain launch per scene and view."""
+    import torch
+
+    scenes = W.batched_scenes(seed=2)
+    jobs, plain = [], []
+    ov = 0
+    for s in scenes:
+        g = ctx.group_create()
+        ctx.group_set_objects(g, s["lower"], s["extent"], s["xform"])
+        ctx.group_set_matrices(g, s["mats"])
+        jobs.append((g, [ctx.result_create(g) for _ in s["vps"]], s["vps"]))
+        plain.append((g, [ctx.result_create(g) for _ in s["vps"]], s["vps"]))
+        ov += len(s["xform"]) * len(s["vps"])
+    p = ctx.plan_create(jobs)
+    tuning = ctx.plan_tuning(p)
+    stream = torch.cuda.ExternalStream(ctx.stream)
+    for _ in range(args.warmup):
+        ctx.plan_launch(p)
+    ctx.synchronize()
+    ev = _events(torch, 4)
+    n = max(3, min(args.steps, 50))
+    with torch.cuda.stream(stream):
+        ev[0].record(stream)
+        for _ in range(n):
+            ctx.plan_launch(p)
+        ev[1].record(stream)
+    ctx.synchronize()
+    batched_ms = ev[0].elapsed_time(ev[1]) / n
+    with torch.cuda.stream(stream):
+        ev[2].record(stream)
+        for _ in range(n):
+            for g, rs, vps in plain:
+                for rr, vp in zip(rs, vps):
+                    ctx.cull(g, rr, vp)
+        ev[3].record(stream)
+    ctx.synchronize()
+    plain_ms = ev[2].elapsed_time(ev[3]) / n
+    for g, _, _ in jobs:
+        ctx.group_destroy(g)
+    return {"workload": f"batched uneven: 256 scenes, {sum(len(s['xform']) for s in scenes)} objects, "
+                        f"{sum(len(s['vps']) for s in scenes)} views",
+            "object_views": ov, "batched_ms": batched_ms, "plain_ms": plain_ms,
+            "batched_object_views_per_s": ov / (batched_ms / 1e3), "plain_object_views_per_s": ov / (plain_ms / 1e3),
+            "batched_vs_plain": plain_ms / batched_ms, "tuning": tuning,
+            "plain_launches_per_step": sum(len(s["vps"]) for s in scenes)}
+
+
 # ---- serving (config 4) ----------------------------------------------------------------------------
 def run_serving(ctx, args) -> dict:
     """64 Poisson clients (mean args.serve_rate requests/s) against a catalogue whose
@@ -429,7 +592,7 @@ def main():
     ap.add_argument("--steps", type=int, default=400)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--workload", default="stress", choices=["stress", "serving"])
+    ap.add_argument("--workload", default="stress", choices=["stress", "serving", "plain", "hierarchy", "batched"])
     ap.add_argument("--tuning", default=None, help="JSON tuning (default: autotuner)")
     ap.add_argument("--cpu-sample", type=int, default=1_000_000)
     ap.add_argument("--objects", type=int, default=STRESS_N, help="objects per GPU (smaller cases for profiling)")
@@ -447,13 +610,14 @@ def main():
     dist = Dist(args.gpus)
     if args.impl == "reference":
         out = run_reference(args, dist)
-    elif args.workload == "serving":
+    elif args.workload in ("serving", "plain", "hierarchy", "batched"):
         from pipeline_gb300 import build, native
 
         build.build_all()
         ctx = native.Context(dist.local)
-        out = {"metric": "serving: p50/p99 request latency and culled object-views/s", "workload": "serving",
-               "serving": run_serving(ctx, args)}
+        fn = {"serving": run_serving, "plain": run_plain_config, "hierarchy": run_hierarchy_config,
+              "batched": run_batched_config}[args.workload]
+        out = {"workload": args.workload, "result": fn(ctx, args)}
         ctx.close()
     else:
         out = run_ours(args, dist)

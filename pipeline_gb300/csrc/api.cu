@@ -144,6 +144,12 @@ struct dpcull_ctx_s {
   uint64_t launches = 0;
   uint64_t device_bytes = 0;
   bool exact_only = false;            // prefilter disabled (testing / ablation)
+  // Upload staging for scatter updates: pinned host and device buffers, grown on demand.
+  unsigned char* stage_h = nullptr;
+  unsigned char* stage_d = nullptr;
+  size_t stage_cap = 0;
+  cudaEvent_t stage_ev = nullptr;
+  bool stage_pending = false;
   std::vector<Group> groups;
   std::vector<Result> results;
   std::vector<Tree> trees;
@@ -364,6 +370,45 @@ CullView view_of(Result& r, const float* vp)
   v.offsets = r.offsets;
   v.n_tiles = r.n_tiles;
   return v;
+}
+
+// Copies n host ranges into the context's pinned staging buffer (after the previous
+// staged copy has left it) and sends them to the device staging buffer in one
+// asynchronous copy; dev[i] receives the device address of part i.  The caller's host
+// memory may be reused as soon as this returns.
+int stage_upload(dpcull_ctx c, int n, const void* const* src, const size_t* bytes, unsigned char** dev)
+{
+  size_t off[8], total = 0;
+  for (int i = 0; i < n; ++i) {
+    off[i] = total;
+    total += (bytes[i] + 255) & ~size_t(255);
+  }
+  if (total > c->stage_cap) {
+    CU(cudaStreamSynchronize(c->stream));
+    if (c->stage_h) cudaFreeHost(c->stage_h);
+    if (c->stage_d) dfree(c, c->stage_d, c->stage_cap);
+    c->stage_h = c->stage_d = nullptr;
+    const size_t cap = std::max(total, 2 * c->stage_cap);
+    c->stage_cap = 0;
+    if (cudaMallocHost((void**)&c->stage_h, cap) != cudaSuccess) {
+      cudaGetLastError();
+      return fail(DPCULL_ERR_NO_MEMORY, "pinned staging allocation failed");
+    }
+    int rc = dalloc(c, (void**)&c->stage_d, cap);
+    if (rc) return rc;
+    c->stage_cap = cap;
+    c->stage_pending = false;
+  }
+  if (!c->stage_ev) CU(cudaEventCreateWithFlags(&c->stage_ev, cudaEventDisableTiming));
+  if (c->stage_pending) CU(cudaEventSynchronize(c->stage_ev));
+  for (int i = 0; i < n; ++i) {
+    memcpy(c->stage_h + off[i], src[i], bytes[i]);
+    dev[i] = c->stage_d + off[i];
+  }
+  CU(cudaMemcpyAsync(c->stage_d, c->stage_h, total, cudaMemcpyHostToDevice, c->stream));
+  CU(cudaEventRecord(c->stage_ev, c->stream));
+  c->stage_pending = true;
+  return DPCULL_OK;
 }
 
 int check_device_errors(dpcull_ctx c)
@@ -594,6 +639,9 @@ int dpcull_ctx_destroy(dpcull_ctx c)
     if (c->groups[g].alive) dpcull_group_destroy(c, g);
   if (c->ctl) cudaFree(c->ctl);
   if (c->h_err) cudaFreeHost(c->h_err);
+  if (c->stage_h) cudaFreeHost(c->stage_h);
+  if (c->stage_d) cudaFree(c->stage_d);
+  if (c->stage_ev) cudaEventDestroy(c->stage_ev);
   if (c->own_stream) cudaStreamDestroy(c->stream);
   delete c;
   return DPCULL_OK;
@@ -706,23 +754,15 @@ int dpcull_group_update_objects(dpcull_ctx c, dpcull_group gh, size_t k, const u
     memcpy(&rows[(3 + r) * k], extent + r * k, k * 4);
   }
   memcpy(&rows[6 * k], xform, k * 4);
-  float* d = nullptr;
-  uint32_t* di = nullptr;
-  int rc = dalloc(c, (void**)&d, rows.size() * 4);
+  const void* src[2] = {rows.data(), index};
+  const size_t bytes[2] = {rows.size() * 4, k * 4};
+  unsigned char* dev[2];
+  int rc = stage_upload(c, 2, src, bytes, dev);
   if (rc) return rc;
-  rc = dalloc(c, (void**)&di, k * 4);
-  if (rc) {
-    dfree(c, d, rows.size() * 4);
-    return rc;
-  }
-  cudaMemcpyAsync(d, rows.data(), rows.size() * 4, cudaMemcpyHostToDevice, c->stream);
-  cudaMemcpyAsync(di, index, k * 4, cudaMemcpyHostToDevice, c->stream);
-  launch_scatter_objects(g->soa, (uint32_t)g->cap, d, di, (uint32_t)k, c->stream);
+  if (launch_scatter_objects(g->soa, (uint32_t)g->cap, reinterpret_cast<float*>(dev[0]),
+                             reinterpret_cast<uint32_t*>(dev[1]), (uint32_t)k, c->stream))
+    return cuda_fail(cudaGetLastError(), "update objects");
   c->launches++;
-  cudaError_t e = cudaStreamSynchronize(c->stream);
-  dfree(c, d, rows.size() * 4);
-  dfree(c, di, k * 4);
-  if (e != cudaSuccess) return cuda_fail(e, "update objects");
   for (size_t i = 0; i < k; ++i) g->xform[index[i]] = xform[i];
   g->max_dirty = true;
   return DPCULL_OK;
@@ -813,23 +853,15 @@ int dpcull_group_update_matrices(dpcull_ctx c, dpcull_group gh, size_t k, const 
     if (index[i] >= g->n_mats) return fail(DPCULL_ERR_OUT_OF_RANGE, "matrix %u >= %zu", index[i], g->n_mats);
     memcpy(&packed[16 * i], (const char*)matrices + (size_t)index[i] * stride, 64);
   }
-  float* d = nullptr;
-  uint32_t* di = nullptr;
-  int rc = dalloc(c, (void**)&d, 64 * k);
+  const void* src[2] = {packed.data(), index};
+  const size_t bytes[2] = {64 * k, 4 * k};
+  unsigned char* dev[2];
+  int rc = stage_upload(c, 2, src, bytes, dev);
   if (rc) return rc;
-  rc = dalloc(c, (void**)&di, 4 * k);
-  if (rc) {
-    dfree(c, d, 64 * k);
-    return rc;
-  }
-  cudaMemcpyAsync(d, packed.data(), 64 * k, cudaMemcpyHostToDevice, c->stream);
-  cudaMemcpyAsync(di, index, 4 * k, cudaMemcpyHostToDevice, c->stream);
-  launch_scatter_matrices(g->mats, d, di, (uint32_t)k, nullptr, c->stream);
+  if (launch_scatter_matrices(g->mats, reinterpret_cast<float*>(dev[0]), reinterpret_cast<uint32_t*>(dev[1]),
+                              (uint32_t)k, nullptr, c->stream))
+    return cuda_fail(cudaGetLastError(), "update matrices");
   c->launches++;
-  cudaError_t e = cudaStreamSynchronize(c->stream);
-  dfree(c, d, 64 * k);
-  dfree(c, di, 4 * k);
-  if (e != cudaSuccess) return cuda_fail(e, "update matrices");
   return DPCULL_OK;
 }
 
@@ -1457,23 +1489,15 @@ static int tree_scatter(dpcull_ctx c, Tree* t, float* dst, size_t k, const uint3
 {
   for (size_t i = 0; i < k; ++i)
     if (index[i] >= t->cap) return fail(DPCULL_ERR_OUT_OF_RANGE, "transform %u >= capacity %zu", index[i], t->cap);
-  float* d = nullptr;
-  uint32_t* di = nullptr;
-  int rc = dalloc(c, (void**)&d, 64 * k);
+  const void* src[2] = {matrices, index};
+  const size_t bytes[2] = {64 * k, 4 * k};
+  unsigned char* dev[2];
+  int rc = stage_upload(c, 2, src, bytes, dev);
   if (rc) return rc;
-  rc = dalloc(c, (void**)&di, 4 * k);
-  if (rc) {
-    dfree(c, d, 64 * k);
-    return rc;
-  }
-  cudaMemcpyAsync(d, matrices, 64 * k, cudaMemcpyHostToDevice, c->stream);
-  cudaMemcpyAsync(di, index, 4 * k, cudaMemcpyHostToDevice, c->stream);
-  launch_scatter_matrices(dst, d, di, (uint32_t)k, dirty, c->stream);
+  if (launch_scatter_matrices(dst, reinterpret_cast<float*>(dev[0]), reinterpret_cast<uint32_t*>(dev[1]),
+                              (uint32_t)k, dirty, c->stream))
+    return cuda_fail(cudaGetLastError(), "tree scatter");
   c->launches++;
-  cudaError_t e = cudaStreamSynchronize(c->stream);
-  dfree(c, d, 64 * k);
-  dfree(c, di, 4 * k);
-  if (e != cudaSuccess) return cuda_fail(e, "tree scatter");
   return DPCULL_OK;
 }
 

@@ -50,7 +50,7 @@ __device__ __forceinline__ uint32_t compu(const uint4& v, int k)
 }
 
 struct CullShared {
-  float vp[kMaxViewsPerPass][16];
+  CullView cv[kMaxViewsPerPass];                     // the item's views (matrices + outputs)
   PfView vn[kMaxViewsPerPass];                       // prefilter view bounds
   uint32_t vis[kMaxViewsPerPass][kTileWords];        // visibility from the exact drain
   uint32_t wtot[kMaxViewsPerPass][kThreads / 32];   // per-warp changed counts
@@ -96,16 +96,19 @@ __device__ void process_item(const CullLaunch& a, uint32_t item, CullShared& sh)
   const int nv = (int)min((uint32_t)VPP, sc.n_views - vfirst);
   const CullView* views = a.views ? a.views + sc.view_begin + vfirst : &a.one_view;
 
-  if (tid < nv * 16) sh.vp[tid >> 4][tid & 15] = views[tid >> 4].vp[tid & 15];
+  // Stage the views (matrices and output pointers) in shared memory: the per-view work
+  // below then never waits on a dependent global load of a descriptor.
+  constexpr int kViewWords = (int)(sizeof(CullView) / 4);
+  static_assert(sizeof(CullView) % 16 == 0, "CullView is staged as whole words");
+  if (tid < nv * kViewWords)
+    reinterpret_cast<uint32_t*>(sh.cv)[tid] = reinterpret_cast<const uint32_t*>(views)[tid];
   if (PF) {
     if (tid < VPP * kTileWords) sh.vis[tid / kTileWords][tid % kTileWords] = 0u;
     if (tid == 0) sh.qn = 0u;
   }
   __syncthreads();
-  if (PF) {
-    if (tid < nv) sh.vn[tid] = pf_view(sh.vp[tid]);
-    __syncthreads();
-  }
+  if (PF && tid < nv) sh.vn[tid] = pf_view(sh.cv[tid].vp);
+  if (PF) __syncthreads();
 
   // ---- visibility of my 4 objects in each view ----
   const uint32_t obj0 = tile * kTileObjects + (uint32_t)tid * kObjPerThread;
@@ -149,7 +152,7 @@ __device__ void process_item(const CullLaunch& a, uint32_t item, CullShared& sh)
 #pragma unroll
     for (int v = 0; v < VPP; ++v) {
       if (v < nv) {
-        const PfViewRegs vr = pf_load_view(sh.vp[v], sh.vn[v]);
+        const PfViewRegs vr = pf_load_view(sh.cv[v].vp, sh.vn[v]);
 #pragma unroll
         for (int k = 0; k < kObjPerThread; ++k) {
           if (valid & (1u << k)) {
@@ -171,7 +174,7 @@ __device__ void process_item(const CullLaunch& a, uint32_t item, CullShared& sh)
                                  comp(ez, k), __ldg(M + 0), __ldg(M + 1), __ldg(M + 2), __ldg(M + 3));
 #pragma unroll
           for (int v = 0; v < VPP; ++v)
-            if (v < nv && obb_visible(o, sh.vp[v])) nib[v] |= 1u << k;
+            if (v < nv && obb_visible(o, sh.cv[v].vp)) nib[v] |= 1u << k;
         } else if (atomicOr(&a.ctl->error, kErrBadTransform) == 0) {
           a.ctl->error_info = obj0 + k;
         }
@@ -204,7 +207,7 @@ __device__ void process_item(const CullLaunch& a, uint32_t item, CullShared& sh)
     for (uint32_t q = tid; q < qn; q += kThreads) {
       const uint32_t e = sh.queue[q];
       const uint32_t o = e >> 3, v = e & 7u;
-      if (exact_visible(sc, tile0 + o, sh.vp[v])) atomicOr(&sh.vis[v][o >> 5], 1u << (o & 31));
+      if (exact_visible(sc, tile0 + o, sh.cv[v].vp)) atomicOr(&sh.vis[v][o >> 5], 1u << (o & 31));
     }
     __syncthreads();
 #pragma unroll
@@ -213,7 +216,13 @@ __device__ void process_item(const CullLaunch& a, uint32_t item, CullShared& sh)
   }
 
   // ---- words, changed nibbles and per-thread changed counts ----
+  // All previous words are loaded before any word is stored, so the loads are in flight
+  // together (a later view's load could not move above an earlier view's store).
   const uint32_t word = tile * kTileWords + (uint32_t)(tid >> 3);
+  uint32_t prevw[VPP];
+#pragma unroll
+  for (int v = 0; v < VPP; ++v)
+    prevw[v] = (v < nv && !(sh.cv[v].flags & kViewNoChanged)) ? sh.cv[v].bits[word] : ~0u;
   const int shift = (tid & 7) * 4;
   uint32_t chg[VPP];
   uint32_t packed[(VPP + 3) / 4];
@@ -223,17 +232,17 @@ __device__ void process_item(const CullLaunch& a, uint32_t item, CullShared& sh)
   for (int v = 0; v < VPP; ++v) {
     chg[v] = 0;
     if (v < nv) {  // nv is uniform over the CTA, so the shuffles stay warp-uniform
-      uint32_t* bits = views[v].bits;
-      const bool track = !(views[v].flags & kViewNoChanged);
-      const uint32_t prev = track ? bits[word] : ~0u;
+      uint32_t* bits = sh.cv[v].bits;
+      const bool track = !(sh.cv[v].flags & kViewNoChanged);
+      const uint32_t prev = prevw[v];
       uint32_t w = nib[v] << shift;
       w |= __shfl_xor_sync(0xffffffffu, w, 1);
       w |= __shfl_xor_sync(0xffffffffu, w, 2);
       w |= __shfl_xor_sync(0xffffffffu, w, 4);
       if ((tid & 7) == 0 && (!track || w != prev)) bits[word] = w;
-      if (views[v].n_visible) {
+      if (sh.cv[v].n_visible) {
         const uint32_t cnt = __reduce_add_sync(0xffffffffu, (uint32_t)__popc(nib[v]));
-        if (lane == 0 && cnt) atomicAdd(views[v].n_visible, cnt);
+        if (lane == 0 && cnt) atomicAdd(sh.cv[v].n_visible, cnt);
       }
       if (track) {
         chg[v] = nib[v] ^ ((prev >> shift) & 0xFu);
@@ -264,7 +273,7 @@ __device__ void process_item(const CullLaunch& a, uint32_t item, CullShared& sh)
   // ---- the tile's changed objects, ascending, into its private slots ----
 #pragma unroll
   for (int v = 0; v < VPP; ++v) {
-    if (v < nv && !(views[v].flags & kViewNoChanged)) {
+    if (v < nv && !(sh.cv[v].flags & kViewNoChanged)) {
       uint32_t before = 0, total = 0;
 #pragma unroll
       for (int w = 0; w < kThreads / 32; ++w) {
@@ -272,11 +281,11 @@ __device__ void process_item(const CullLaunch& a, uint32_t item, CullShared& sh)
         before += w < warp ? t : 0u;
         total += t;
       }
-      if (tid == 0) views[v].counts[tile] = total;
+      if (tid == 0) sh.cv[v].counts[tile] = total;
       if (chg[v]) {
         const uint32_t own = (uint32_t)__popc(chg[v]);
         uint32_t off = tile * kTileObjects + before + ((incl[v >> 2] >> (8 * (v & 3))) & 0xFFu) - own;
-        uint32_t* slots = views[v].slots;
+        uint32_t* slots = sh.cv[v].slots;
         uint32_t m = chg[v];
         while (m) {
           const int k = __ffs(m) - 1;

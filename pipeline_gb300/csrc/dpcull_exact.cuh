@@ -7,6 +7,8 @@
 // rows, row-major, row-vector convention (v' = v * M).
 #pragma once
 
+#include <cstdint>
+
 #include <cuda_runtime.h>
 
 namespace dpcull {

@@ -43,7 +43,7 @@ struct CullScene {
   uint32_t item_begin;     // first work item of this scene (items = tiles x view groups)
 };
 
-struct CullView {
+struct alignas(16) CullView {   // 128 bytes; staged whole into shared memory by the cull
   float vp[16];
   uint32_t* bits;        // previous visibility on entry, new visibility on exit
   uint32_t* changed;     // ascending changed-object list
