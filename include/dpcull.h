@@ -150,7 +150,7 @@ typedef struct dpcull_job {
 
 typedef struct dpcull_tuning {
   uint32_t views_per_pass;   /* 1, 2, 4 or 8 views evaluated per object load ("views per warp") */
-  uint32_t tiles_per_ticket; /* tiles a CTA claims at once ("tiles per CTA") */
+  uint32_t tiles_per_ticket; /* 512-object work items a warp claims at once ("tiles per CTA") */
   uint32_t ctas_per_sm;      /* persistent CTAs per SM (0 = occupancy limit) */
   uint32_t reserved;
 } dpcull_tuning;
@@ -272,12 +272,12 @@ int dpcull_server_get_stats(dpcull_server s, dpcull_server_stats* out);
  * cudaMalloc's implicit device synchronisation, or a process whose device memory is all
  * owned by another allocator (a framework's caching allocator, a budget reserved up
  * front).  It runs the plain cull of dpcull_cull on buffers the caller owns and takes its
- * scratch from one static device array of about 4 MB that every GPU loading this
+ * scratch from one static device array of about 128 KB that every GPU loading this
  * library holds until the process exits; it calls no cudaMalloc, cudaFree or other
  * allocating routine.
  *   objects   device, 16-byte aligned: 7 rows of `cap` entries -- lower x, y, z,
  *             extent x, y, z (float) and the transform index (uint32);
- *             cap is a multiple of 1024 and >= n; n <= DPCULL_NOALLOC_MAX_OBJECTS
+ *             cap is a multiple of 128 and >= n; n <= DPCULL_NOALLOC_MAX_OBJECTS
  *             (larger n: DPCULL_ERR_CAPACITY)
  *   matrices  device, 16-byte aligned, n_matrices x 16 floats
  *   bits      device, cap/32 words: the previous visibility on entry (a result that was

@@ -84,11 +84,9 @@ struct Result {
   uint32_t* changed = nullptr;
   size_t changed_cap = 0;
   uint32_t* n_changed = nullptr;
-  uint32_t* slots = nullptr;        // tiles_cap x kTileObjects
-  uint32_t* counts = nullptr;       // tiles_cap
-  uint32_t* offsets = nullptr;      // tiles_cap
-  size_t tiles_cap = 0;
-  uint32_t n_tiles = 0;             // tiles of the group at the last prepare
+  uint32_t* delta = nullptr;        // words_cap: old XOR new visibility (changed-list scratch)
+  uint32_t* chunk_tot = nullptr;    // chunks_of(words_cap): changed objects per chunk
+  uint32_t n_words = 0;             // visibility words of the group at the last prepare
 };
 
 struct TreeLaunch {
@@ -297,7 +295,14 @@ int result_prepare(dpcull_ctx c, Result& r, Group& g)
       dfree(c, r.bits, r.words_cap * 4);
     }
     r.bits = nb;
+    CU(cudaStreamSynchronize(c->stream));
+    dfree(c, r.delta, r.words_cap * 4);
+    dfree(c, r.chunk_tot, chunks_of(r.words_cap) * 4);
+    r.delta = r.chunk_tot = nullptr;
     r.words_cap = words;
+    rc = dalloc(c, (void**)&r.delta, words * 4);
+    if (!rc) rc = dalloc(c, (void**)&r.chunk_tot, chunks_of(words) * 4);
+    if (rc) return rc;
   }
   const size_t chcap = std::max<size_t>(g.n, 1);
   if (chcap > r.changed_cap) {
@@ -309,26 +314,7 @@ int result_prepare(dpcull_ctx c, Result& r, Group& g)
     if (rc) return rc;
     r.changed_cap = want;
   }
-  if (std::max<size_t>(tiles, 1) > r.tiles_cap) {
-    CU(cudaStreamSynchronize(c->stream));
-    dfree(c, r.slots, r.tiles_cap * kTileObjects * 4);
-    dfree(c, r.counts, r.tiles_cap * 4);
-    dfree(c, r.offsets, r.tiles_cap * 4);
-    r.slots = r.counts = r.offsets = nullptr;
-    const size_t want = std::max<size_t>(tiles, r.tiles_cap + r.tiles_cap / 2);
-    r.tiles_cap = 0;
-    int rc = dalloc(c, (void**)&r.slots, want * kTileObjects * 4);
-    if (!rc) rc = dalloc(c, (void**)&r.counts, want * 4);
-    if (!rc) rc = dalloc(c, (void**)&r.offsets, want * 4);
-    if (rc) {
-      dfree(c, r.slots, want * kTileObjects * 4);
-      dfree(c, r.counts, want * 4);
-      r.slots = r.counts = nullptr;
-      return rc;
-    }
-    r.tiles_cap = want;
-  }
-  r.n_tiles = tiles;
+  r.n_words = tiles * kTileWords;
   if (r.incarnation != g.incarnation) {
     r.incarnation = g.incarnation;
     const size_t old = r.size_bits;
@@ -365,10 +351,9 @@ CullView view_of(Result& r, const float* vp)
   v.bits = r.bits;
   v.changed = r.changed;
   v.n_changed = r.n_changed;
-  v.slots = r.slots;
-  v.counts = r.counts;
-  v.offsets = r.offsets;
-  v.n_tiles = r.n_tiles;
+  v.delta = r.delta;
+  v.chunk_tot = r.chunk_tot;
+  v.n_words = r.n_words;
   return v;
 }
 
@@ -466,7 +451,7 @@ int build_batch(dpcull_ctx c, const dpcull_job* jobs, size_t n_jobs, uint32_t vp
       if (results_out) results_out->push_back(jobs[j].results[v]);
     }
     CullScene s = scene_of(*g, vb, jobs[j].n_views, vpp, items);
-    items += s.n_tiles * s.n_vgroups;
+    items += items_of(s.n_tiles, s.n_vgroups);
     scenes.push_back(s);
     if (groups_out) groups_out->push_back(jobs[j].group);
   }
@@ -479,14 +464,15 @@ int persistent_grid(dpcull_ctx c, uint32_t vpp, uint32_t ctas_per_sm, uint32_t n
 {
   int occ = cull_max_ctas_per_sm((int)vpp);
   int per_sm = ctas_per_sm ? std::min<int>((int)ctas_per_sm, occ) : occ;
-  long long want = ((long long)n_items + per_ticket - 1) / per_ticket;
+  const long long per_cta = (long long)per_ticket * kWarpsPerCta;  // each warp claims its own
+  long long want = ((long long)n_items + per_cta - 1) / per_cta;
   long long grid = std::min<long long>((long long)c->sm_count * per_sm, want);
   return (int)std::max<long long>(grid, 1);
 }
 
 // The cull over all scenes and views, then the changed-list assembly of every view.
 int launch_batch(dpcull_ctx c, const CullScene* d_scenes, const CullView* d_views,
-                 uint32_t n_scenes, uint32_t n_views, uint32_t max_tiles, uint32_t n_items,
+                 uint32_t n_scenes, uint32_t n_views, uint32_t max_words, uint32_t n_items,
                  const dpcull_tuning& t, cudaStream_t s)
 {
   if (n_views > 65535) return fail(DPCULL_ERR_INVALID_ARGUMENT, "at most 65535 views per launch");
@@ -501,16 +487,16 @@ int launch_batch(dpcull_ctx c, const CullScene* d_scenes, const CullView* d_view
   const int grid = persistent_grid(c, t.views_per_pass, t.ctas_per_sm, n_items, a.items_per_ticket);
   if (launch_cull(a, grid, (int)t.views_per_pass, s)) return cuda_fail(cudaGetLastError(), "cull launch");
   CullView none{};
-  if (launch_changed_lists(d_views, none, n_views, max_tiles, s))
+  if (launch_changed_lists(d_views, none, n_views, max_words, s))
     return cuda_fail(cudaGetLastError(), "changed-list launch");
   c->launches += 3;
   return DPCULL_OK;
 }
 
-uint32_t max_tiles_of(const std::vector<CullScene>& scenes)
+uint32_t max_words_of(const std::vector<CullScene>& scenes)
 {
   uint32_t m = 1;
-  for (auto& s : scenes) m = std::max(m, s.n_tiles);
+  for (auto& s : scenes) m = std::max(m, s.n_tiles * (uint32_t)kTileWords);
   return m;
 }
 
@@ -526,7 +512,8 @@ std::string tune_key(const std::vector<CullScene>& scenes, const std::vector<Cul
   }
   const int bucket = objs ? (int)std::floor(std::log2((double)objs)) : 0;
   char buf[96];
-  snprintf(buf, sizeof buf, "n2^%d_v%zu_maxv%u_s%zu", bucket, views.size(), maxv, scenes.size());
+  // "w512": tunings of the kernel whose warp items are 512 objects
+  snprintf(buf, sizeof buf, "w512_n2^%d_v%zu_maxv%u_s%zu", bucket, views.size(), maxv, scenes.size());
   return buf;
 }
 
@@ -938,9 +925,8 @@ int dpcull_result_destroy(dpcull_ctx c, dpcull_result rh)
   dfree(c, r->bits, r->words_cap * 4);
   dfree(c, r->changed, r->changed_cap * 4);
   dfree(c, r->n_changed, 4);
-  dfree(c, r->slots, r->tiles_cap * kTileObjects * 4);
-  dfree(c, r->counts, r->tiles_cap * 4);
-  dfree(c, r->offsets, r->tiles_cap * 4);
+  dfree(c, r->delta, r->words_cap * 4);
+  dfree(c, r->chunk_tot, chunks_of(r->words_cap) * 4);
   if (r->group < c->groups.size()) {
     auto& v = c->groups[r->group].results;
     v.erase(std::remove(v.begin(), v.end(), rh), v.end());
@@ -972,9 +958,10 @@ int dpcull_cull(dpcull_ctx c, dpcull_group gh, dpcull_result rh, const float vp[
   a.ctl = c->ctl;
   a.one_scene = scene_of(*g, 0, 1, 1, 0);
   a.one_view = view_of(*r, vp);
-  a.n_items = a.one_scene.n_tiles;
-  if (launch_cull(a, (int)a.n_items, 1, c->stream)) return cuda_fail(cudaGetLastError(), "cull launch");
-  if (launch_changed_lists(nullptr, a.one_view, 1, a.one_scene.n_tiles, c->stream))
+  a.n_items = items_of(a.one_scene.n_tiles, 1);
+  const int grid = persistent_grid(c, 1, 0, a.n_items, 1);
+  if (launch_cull(a, grid, 1, c->stream)) return cuda_fail(cudaGetLastError(), "cull launch");
+  if (launch_changed_lists(nullptr, a.one_view, 1, a.one_view.n_words, c->stream))
     return cuda_fail(cudaGetLastError(), "changed-list launch");
   c->launches += 3;
   return DPCULL_OK;
@@ -1079,7 +1066,7 @@ int dpcull_cull_batched(dpcull_ctx c, const dpcull_job* jobs, size_t n_jobs, con
   }
   cudaMemcpyAsync(ds, scenes.data(), scenes.size() * sizeof(CullScene), cudaMemcpyHostToDevice, c->stream);
   cudaMemcpyAsync(dv, views.data(), views.size() * sizeof(CullView), cudaMemcpyHostToDevice, c->stream);
-  rc = launch_batch(c, ds, dv, (uint32_t)scenes.size(), (uint32_t)views.size(), max_tiles_of(scenes),
+  rc = launch_batch(c, ds, dv, (uint32_t)scenes.size(), (uint32_t)views.size(), max_words_of(scenes),
                     items, t, c->stream);
   cudaStreamSynchronize(c->stream);
   dfree(c, ds, scenes.size() * sizeof(CullScene));
@@ -1100,7 +1087,7 @@ static int plan_capture(dpcull_ctx c, Plan& p, int slot)
   if (e == cudaSuccess) {
     const uint64_t before = c->launches;
     rc = launch_batch(c, p.d_scenes, p.d_views, (uint32_t)p.scenes.size(), (uint32_t)p.views.size(),
-                      max_tiles_of(p.scenes), p.n_items, p.tuning, cs);
+                      max_words_of(p.scenes), p.n_items, p.tuning, cs);
     c->launches = before;  // counted when the graph is replayed
   }
   cudaError_t e2 = cudaStreamEndCapture(cs, &graph);
@@ -1120,7 +1107,7 @@ static int time_batch(dpcull_ctx c, const CullScene* ds, const CullView* dv,
   cudaEvent_t e0, e1;
   CU(cudaEventCreate(&e0));
   CU(cudaEventCreate(&e1));
-  const uint32_t ns = (uint32_t)sc.size(), nvw = (uint32_t)vw.size(), mt = max_tiles_of(sc);
+  const uint32_t ns = (uint32_t)sc.size(), nvw = (uint32_t)vw.size(), mt = max_words_of(sc);
   int rc = launch_batch(c, ds, dv, ns, nvw, mt, items, t, c->stream);  // warm-up
   if (!rc) cudaEventRecord(e0, c->stream);
   for (int i = 0; i < reps && !rc; ++i) rc = launch_batch(c, ds, dv, ns, nvw, mt, items, t, c->stream);

@@ -1,29 +1,29 @@
 // cull.cu -- frustum-cull kernels of the GB300 culling backend.
 //
-// One kernel serves both the plain per-call path (one group, one view, a grid of one
-// CTA per tile) and the batched persistent path (many groups x many views, a grid of
-// resident CTAs that pull work items from an atomic ticket).  A work item is one tile of
-// 1024 objects of one scene and one group of up to VPP views:
-//   1. stage the views' view-projection matrices (and their prefilter bounds) in shared
-//      memory;
-//   2. 128-bit streaming loads of the tile's SoA rows (each thread owns 4 objects);
-//   3. per object: gather its world matrix (4 x 128-bit __ldg) and build the world-space
-//      box exactly as the reference's OBB cache; per view, the conservative prefilter
-//      (dpcull_exact.cuh) decides visible / invisible where the reference's rounded
-//      result is certain; the undecided (object, view) pairs of the tile are compacted
-//      into a shared-memory queue and run through the exact reference test by all
-//      threads together, so no warp idles on a rare exact pair;
-//   4. per view: assemble the 32-bit visibility words with warp shuffles, XOR them with
-//      the result's previous words (ResultBitSet::updateChanged), write the new words
-//      (only where they changed), and write the tile's changed objects, ascending, into
-//      the tile's private slot range together with the tile's count.
-// A CTA never waits for another.  Two small kernels then turn the per-tile slots into
-// the packed ascending changed list: a per-view exclusive scan of the tile counts and a
-// gather of the slots (launch_changed_lists).
+// One kernel serves the plain per-call path (one group, one view) and the batched
+// persistent path (many groups x many views).  Every warp works on its own: it pulls work
+// items from an atomic ticket, and a work item is up to 4 tiles of 128 objects (one
+// float4 of each SoA row per lane) of one scene with one group of up to VPP views:
+//   1. stage the views (view-projection matrices, output pointers) and their prefilter
+//      planes in the warp's shared memory, unless the previous item had the same views;
+//   2. per tile: 128-bit streaming loads of the SoA rows; per object, gather its world
+//      matrix (4 x 128-bit __ldg) and build its prefilter box; per view, the
+//      conservative prefilter (dpcull_prefilter.h) decides visible / invisible wherever
+//      the reference's rounded result is certain; the decided-visible words go to shared
+//      memory and the undecided (object, view) pairs to the warp's queue;
+//   3. all lanes run the queued pairs through the exact reference test (dpcull_exact.cuh)
+//      and set the visible ones in the words;
+//   4. per tile and view: XOR with the result's previous words (ResultBitSet::
+//      updateChanged), store the new words where they changed and the delta words.
+// No warp waits for another.  Two small kernels then turn the delta words into the packed
+// ascending changed list (launch_changed_lists).
+#include <algorithm>
+
 #include <cuda_runtime.h>
 
 #include "dpcull_exact.cuh"
 #include "dpcull_internal.h"
+#include "dpcull_prefilter.h"
 
 namespace dpcull {
 
@@ -49,15 +49,18 @@ __device__ __forceinline__ uint32_t compu(const uint4& v, int k)
   return k == 0 ? v.x : k == 1 ? v.y : k == 2 ? v.z : v.w;
 }
 
-struct CullShared {
-  CullView cv[kMaxViewsPerPass];                     // the item's views (matrices + outputs)
-  PfView vn[kMaxViewsPerPass];                       // prefilter view bounds
-  uint32_t vis[kMaxViewsPerPass][kTileWords];        // visibility from the exact drain
-  uint32_t wtot[kMaxViewsPerPass][kThreads / 32];   // per-warp changed counts
-  uint32_t item;
-  uint32_t qn;                                       // undecided (object, view) pairs
-  uint16_t queue[kTileObjects * kMaxViewsPerPass];   // entry = tile object << 3 | view
+// Shared memory of one warp: its cached scene and views, the views' prefilter planes, the
+// provisional visibility words of its item and the item's undecided pairs.  Warps of a
+// CTA never share state, so no CTA barrier is taken per item.
+struct WarpShared {
+  CullScene sc;                                          // the scene of the warp's last item
+  CullView cv[kMaxViewsPerPass];                         // the item's views (matrices + outputs)
+  pf::Planes pl[kMaxViewsPerPass];                       // prefilter planes of the views
+  uint32_t words[kItemTiles][kMaxViewsPerPass][kTileWords];  // the item's visibility words
+  uint16_t queue[kQueueCap];                             // tile << 10 | object << 3 | view
 };
+static_assert(kTileObjects == 32 * kObjPerThread, "a tile is one warp's objects");
+static_assert(kItemTiles * kMaxViewsPerPass * kTileWords == 4 * 32, "four words per lane");
 
 __device__ __forceinline__ uint32_t find_scene(const CullScene* scenes, uint32_t n, uint32_t item)
 {
@@ -85,33 +88,77 @@ __device__ __forceinline__ bool exact_visible(const CullScene& sc, uint32_t i, c
   return obb_visible(o, vp);
 }
 
-template <int VPP, bool PF>
-__device__ void process_item(const CullLaunch& a, uint32_t item, CullShared& sh)
+// Prefilter of the lane's 4 boxes in each view of the item: visible objects into nib[v]
+// (bit k), undecided pairs into amb (bit 8k + v).  Branch-free per pair.
+template <int VPP, bool kAffine>
+__device__ __forceinline__ void classify_views(const WarpShared& ws, const pf::Box (&bx)[kObjPerThread],
+                                               int nv, uint32_t valid, uint32_t (&nib)[VPP],
+                                               uint32_t& amb)
 {
-  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-  const CullScene sc = a.scenes ? a.scenes[find_scene(a.scenes, a.n_scenes, item)] : a.one_scene;
-  const uint32_t local = item - sc.item_begin;
-  const uint32_t tile = local / sc.n_vgroups;
-  const uint32_t vfirst = (local - tile * sc.n_vgroups) * VPP;
-  const int nv = (int)min((uint32_t)VPP, sc.n_views - vfirst);
-  const CullView* views = a.views ? a.views + sc.view_begin + vfirst : &a.one_view;
-
-  // Stage the views (matrices and output pointers) in shared memory: the per-view work
-  // below then never waits on a dependent global load of a descriptor.
-  constexpr int kViewWords = (int)(sizeof(CullView) / 4);
-  static_assert(sizeof(CullView) % 16 == 0, "CullView is staged as whole words");
-  if (tid < nv * kViewWords)
-    reinterpret_cast<uint32_t*>(sh.cv)[tid] = reinterpret_cast<const uint32_t*>(views)[tid];
-  if (PF) {
-    if (tid < VPP * kTileWords) sh.vis[tid / kTileWords][tid % kTileWords] = 0u;
-    if (tid == 0) sh.qn = 0u;
+#pragma unroll
+  for (int v = 0; v < VPP; ++v) {
+    if (v < nv) {
+      const pf::Planes& P = ws.pl[v];
+      const float rho = P.rho.x;
+      float mi[kObjPerThread], mo[kObjPerThread];
+#pragma unroll
+      for (int k = 0; k < kObjPerThread; ++k) mi[k] = mo[k] = __int_as_float(0x7f800000);
+#pragma unroll
+      for (int ax = 0; ax < 3; ++ax) {
+        const pf::F4 ql = P.q[ax][0], qh = P.q[ax][1], nm = P.nm[ax];
+#pragma unroll
+        for (int k = 0; k < kObjPerThread; ++k) pf::axis<kAffine>(bx[k], ql, qh, nm, mi[k], mo[k]);
+      }
+      uint32_t in = 0, und = 0;
+#pragma unroll
+      for (int k = 0; k < kObjPerThread; ++k) {
+        const float d = fmaf(bx[k].dw, rho, bx[k].d0);
+        const bool vis = mi[k] > d, out = mo[k] <= -d;
+        in |= (uint32_t)vis << k;
+        und |= (uint32_t)(!vis && !out) << k;
+      }
+      nib[v] = in & valid;
+      // bit k of und -> bit 8k (the multiply places each bit k at 8k; the mask drops the
+      // cross terms), then view v's column
+      amb |= (((und & valid) * 0x204081u) & 0x01010101u) << v;
+    }
   }
-  __syncthreads();
-  if (PF && tid < nv) sh.vn[tid] = pf_view(sh.cv[tid].vp);
-  if (PF) __syncthreads();
+}
 
-  // ---- visibility of my 4 objects in each view ----
-  const uint32_t obj0 = tile * kTileObjects + (uint32_t)tid * kObjPerThread;
+// Inclusive warp scan.
+__device__ __forceinline__ uint32_t warp_scan(uint32_t x, int lane)
+{
+#pragma unroll
+  for (int d = 1; d < 32; d <<= 1) {
+    const uint32_t y = __shfl_up_sync(0xffffffffu, x, d);
+    if (lane >= d) x += y;
+  }
+  return x;
+}
+
+// Runs the queued undecided pairs through the exact test, all lanes together, and sets
+// the visible ones in the item's words.
+__device__ __forceinline__ void drain_queue(WarpShared& ws, const CullScene& sc, uint32_t tile_first,
+                                            uint32_t qn, int lane)
+{
+  __syncwarp();
+  for (uint32_t q = lane; q < qn; q += 32) {
+    const uint32_t e = ws.queue[q];
+    const uint32_t t = e >> 10, o = (e >> 3) & 127u, v = e & 7u;
+    if (exact_visible(sc, (tile_first + t) * kTileObjects + o, ws.cv[v].vp))
+      atomicOr(&ws.words[t][v][o >> 5], 1u << (o & 31));
+  }
+  __syncwarp();
+}
+
+// Classification of one tile into the item's words (visible objects) and queue
+// (undecided pairs).  Returns the new queue length.
+template <int VPP, bool PF>
+__device__ __forceinline__ uint32_t classify_tile(const CullLaunch& a, WarpShared& ws, const CullScene& sc,
+                                                  uint32_t tile, uint32_t t, uint32_t tile_first,
+                                                  int nv, uint32_t qn, int lane)
+{
+  const uint32_t obj0 = tile * kTileObjects + (uint32_t)lane * kObjPerThread;
   const float* soa = sc.soa;
   const size_t cap = sc.cap;
   const float4 lx = ld_stream4(soa + 0 * cap + obj0);
@@ -126,43 +173,39 @@ __device__ void process_item(const CullLaunch& a, uint32_t item, CullShared& sh)
   uint32_t nib[VPP];
 #pragma unroll
   for (int v = 0; v < VPP; ++v) nib[v] = 0;
-  uint32_t amb = 0;  // bit 8k + v: object k in view v needs the exact test
+  uint32_t amb = 0;
 
   if (PF) {
-    // Boxes and their bounds for the 4 objects first (the 16 matrix gathers overlap),
-    // then each view's constants are read once for all 4 objects.
-    PfObject pb[kObjPerThread];
+    // Prefilter boxes of the 4 objects first (the 16 matrix gathers overlap), then each
+    // view's planes are read once for all 4 objects.
+    pf::Box bx[kObjPerThread];
     uint32_t valid = 0;
+    bool affine = true;
 #pragma unroll
     for (int k = 0; k < kObjPerThread; ++k) {
-      pb[k].da = pf_nan();
-      if (obj0 + k < sc.n_objects) {
-        const uint32_t mi = compu(xf, k);
-        if (mi < sc.n_mats) {
-          const float4* M = mats + 4 * (size_t)mi;
-          const Obb o = make_obb(comp(lx, k), comp(ly, k), comp(lz, k), comp(ex, k), comp(ey, k),
-                                 comp(ez, k), __ldg(M + 0), __ldg(M + 1), __ldg(M + 2), __ldg(M + 3));
-          pb[k] = pf_object(o);
-          valid |= 1u << k;
-        } else if (atomicOr(&a.ctl->error, kErrBadTransform) == 0) {
-          a.ctl->error_info = obj0 + k;
-        }
+      const uint32_t mi = compu(xf, k);
+      const bool exists = obj0 + k < sc.n_objects;
+      const bool use = exists && mi < sc.n_mats;
+      if (exists && !use && atomicOr(&a.ctl->error, kErrBadTransform) == 0) a.ctl->error_info = obj0 + k;
+      float4 r0 = make_float4(0.f, 0.f, 0.f, 0.f), r1 = r0, r2 = r0, r3 = r0;
+      if (use) {
+        const float4* M = mats + 4 * (size_t)mi;
+        r0 = __ldg(M + 0);
+        r1 = __ldg(M + 1);
+        r2 = __ldg(M + 2);
+        r3 = __ldg(M + 3);
       }
+      const pf::F4 m0{r0.x, r0.y, r0.z, r0.w}, m1{r1.x, r1.y, r1.z, r1.w};
+      const pf::F4 m2{r2.x, r2.y, r2.z, r2.w}, m3{r3.x, r3.y, r3.z, r3.w};
+      bx[k] = pf::make_box(comp(lx, k), comp(ly, k), comp(lz, k), comp(ex, k), comp(ey, k),
+                           comp(ez, k), m0, m1, m2, m3);
+      affine = affine && (!use || pf::is_affine(m0, m1, m2, m3));
+      valid |= (uint32_t)use << k;
     }
-#pragma unroll
-    for (int v = 0; v < VPP; ++v) {
-      if (v < nv) {
-        const PfViewRegs vr = pf_load_view(sh.cv[v].vp, sh.vn[v]);
-#pragma unroll
-        for (int k = 0; k < kObjPerThread; ++k) {
-          if (valid & (1u << k)) {
-            const int cls = pf_classify(pb[k], vr);
-            if (cls == kPfVisible) nib[v] |= 1u << k;
-            else if (cls == kPfAmbiguous) amb |= 1u << (8 * k + v);
-          }
-        }
-      }
-    }
+    // Affine world matrices (c.w == 1, no w extent) take the shorter plane test; the
+    // choice is uniform over the warp.
+    if (__all_sync(0xffffffffu, affine)) classify_views<VPP, true>(ws, bx, nv, valid, nib, amb);
+    else classify_views<VPP, false>(ws, bx, nv, valid, nib, amb);
   } else {
 #pragma unroll
     for (int k = 0; k < kObjPerThread; ++k) {
@@ -174,7 +217,7 @@ __device__ void process_item(const CullLaunch& a, uint32_t item, CullShared& sh)
                                  comp(ez, k), __ldg(M + 0), __ldg(M + 1), __ldg(M + 2), __ldg(M + 3));
 #pragma unroll
           for (int v = 0; v < VPP; ++v)
-            if (v < nv && obb_visible(o, sh.cv[v].vp)) nib[v] |= 1u << k;
+            if (v < nv && obb_visible(o, ws.cv[v].vp)) nib[v] |= 1u << k;
         } else if (atomicOr(&a.ctl->error, kErrBadTransform) == 0) {
           a.ctl->error_info = obj0 + k;
         }
@@ -182,136 +225,148 @@ __device__ void process_item(const CullLaunch& a, uint32_t item, CullShared& sh)
     }
   }
 
-  if (PF) {
-    // ---- compact the undecided pairs of the tile and run them through the exact test ----
-    const uint32_t cnt = (uint32_t)__popc(amb);
-    uint32_t x = cnt;
-#pragma unroll
-    for (int d = 1; d < 32; d <<= 1) {
-      const uint32_t y = __shfl_up_sync(0xffffffffu, x, d);
-      if (lane >= d) x += y;
-    }
-    uint32_t base = 0;
-    if (lane == 31) base = atomicAdd(&sh.qn, x);
-    base = __shfl_sync(0xffffffffu, base, 31);
-    uint32_t pos = base + x - cnt;
-    while (amb) {
-      const int b = __ffs(amb) - 1;
-      sh.queue[pos++] =
-          (uint16_t)(((uint32_t)(tid * kObjPerThread + (b >> 3)) << 3) | (uint32_t)(b & 7));
-      amb &= amb - 1u;
-    }
-    __syncthreads();
-    const uint32_t qn = sh.qn;
-    const uint32_t tile0 = tile * kTileObjects;
-    for (uint32_t q = tid; q < qn; q += kThreads) {
-      const uint32_t e = sh.queue[q];
-      const uint32_t o = e >> 3, v = e & 7u;
-      if (exact_visible(sc, tile0 + o, sh.cv[v].vp)) atomicOr(&sh.vis[v][o >> 5], 1u << (o & 31));
-    }
-    __syncthreads();
-#pragma unroll
-    for (int v = 0; v < VPP; ++v)
-      if (v < nv) nib[v] |= (sh.vis[v][tid >> 3] >> ((tid & 7) * 4)) & 0xFu;
-  }
-
-  // ---- words, changed nibbles and per-thread changed counts ----
-  // All previous words are loaded before any word is stored, so the loads are in flight
-  // together (a later view's load could not move above an earlier view's store).
-  const uint32_t word = tile * kTileWords + (uint32_t)(tid >> 3);
-  uint32_t prevw[VPP];
-#pragma unroll
-  for (int v = 0; v < VPP; ++v)
-    prevw[v] = (v < nv && !(sh.cv[v].flags & kViewNoChanged)) ? sh.cv[v].bits[word] : ~0u;
-  const int shift = (tid & 7) * 4;
-  uint32_t chg[VPP];
-  uint32_t packed[(VPP + 3) / 4];
-#pragma unroll
-  for (int q = 0; q < (VPP + 3) / 4; ++q) packed[q] = 0;
+  // The decided-visible words of the tile (warp shuffles), into the item's words.
+  const int shift = (lane & 7) * 4;
 #pragma unroll
   for (int v = 0; v < VPP; ++v) {
-    chg[v] = 0;
-    if (v < nv) {  // nv is uniform over the CTA, so the shuffles stay warp-uniform
-      uint32_t* bits = sh.cv[v].bits;
-      const bool track = !(sh.cv[v].flags & kViewNoChanged);
-      const uint32_t prev = prevw[v];
+    if (v < nv) {  // nv is uniform over the warp, so the shuffles stay warp-uniform
       uint32_t w = nib[v] << shift;
       w |= __shfl_xor_sync(0xffffffffu, w, 1);
       w |= __shfl_xor_sync(0xffffffffu, w, 2);
       w |= __shfl_xor_sync(0xffffffffu, w, 4);
-      if ((tid & 7) == 0 && (!track || w != prev)) bits[word] = w;
-      if (sh.cv[v].n_visible) {
-        const uint32_t cnt = __reduce_add_sync(0xffffffffu, (uint32_t)__popc(nib[v]));
-        if (lane == 0 && cnt) atomicAdd(sh.cv[v].n_visible, cnt);
-      }
-      if (track) {
-        chg[v] = nib[v] ^ ((prev >> shift) & 0xFu);
-        packed[v >> 2] |= (uint32_t)__popc(chg[v]) << (8 * (v & 3));
-      }
+      if ((lane & 7) == 0) ws.words[t][v][lane >> 3] = w;
     }
   }
 
-  // Warp inclusive scan of the packed counts (fields stay below 256: 32 lanes x 4).
-  uint32_t incl[(VPP + 3) / 4];
-#pragma unroll
-  for (int q = 0; q < (VPP + 3) / 4; ++q) {
-    uint32_t x = packed[q];
-#pragma unroll
-    for (int d = 1; d < 32; d <<= 1) {
-      const uint32_t y = __shfl_up_sync(0xffffffffu, x, d);
-      if (lane >= d) x += y;
+  // The undecided pairs into the queue (drained early only if it would overflow).
+  if (PF) {
+    const uint32_t cnt = (uint32_t)__popc(amb);
+    const uint32_t incl = warp_scan(cnt, lane);
+    const uint32_t tot = __shfl_sync(0xffffffffu, incl, 31);
+    if (tot) {  // uniform over the warp
+      if (qn + tot > (uint32_t)kQueueCap) {
+        drain_queue(ws, sc, tile_first, qn, lane);
+        qn = 0;
+      }
+      uint32_t pos = qn + incl - cnt;
+      while (amb) {
+        const int b = __ffs(amb) - 1;
+        ws.queue[pos++] = (uint16_t)((t << 10) | ((uint32_t)(lane * kObjPerThread + (b >> 3)) << 3) | (uint32_t)(b & 7));
+        amb &= amb - 1u;
+      }
+      qn += tot;
     }
-    incl[q] = x;
   }
-  if (lane == 31) {
-#pragma unroll
-    for (int v = 0; v < VPP; ++v)
-      if (v < nv) sh.wtot[v][warp] = (incl[v >> 2] >> (8 * (v & 3))) & 0xFFu;
-  }
-  __syncthreads();
+  return qn;
+}
 
-  // ---- the tile's changed objects, ascending, into its private slots ----
+// The final words of one tile of the item: the new words (stored only where they
+// changed), the delta words (old XOR new, every word) and the visible counts.
+template <int VPP>
+__device__ __forceinline__ void finish_tile(const WarpShared& ws, uint32_t tile, uint32_t t, int nv, int lane)
+{
+  const uint32_t word = tile * kTileWords + (uint32_t)(lane >> 3);
+  const bool writer = (lane & 7) == 0;  // lanes 0, 8, 16, 24 own the tile's 4 words
+  // All previous words are loaded before any word is stored, so the loads are in flight
+  // together (a later view's load could not move above an earlier view's store).
+  uint32_t prevw[VPP];
+#pragma unroll
+  for (int v = 0; v < VPP; ++v)
+    prevw[v] = (v < nv && writer && !(ws.cv[v].flags & kViewNoChanged)) ? ws.cv[v].bits[word] : 0u;
 #pragma unroll
   for (int v = 0; v < VPP; ++v) {
-    if (v < nv && !(sh.cv[v].flags & kViewNoChanged)) {
-      uint32_t before = 0, total = 0;
-#pragma unroll
-      for (int w = 0; w < kThreads / 32; ++w) {
-        const uint32_t t = sh.wtot[v][w];
-        before += w < warp ? t : 0u;
-        total += t;
-      }
-      if (tid == 0) sh.cv[v].counts[tile] = total;
-      if (chg[v]) {
-        const uint32_t own = (uint32_t)__popc(chg[v]);
-        uint32_t off = tile * kTileObjects + before + ((incl[v >> 2] >> (8 * (v & 3))) & 0xFFu) - own;
-        uint32_t* slots = sh.cv[v].slots;
-        uint32_t m = chg[v];
-        while (m) {
-          const int k = __ffs(m) - 1;
-          slots[off++] = obj0 + (uint32_t)k;
-          m &= m - 1u;
+    if (v < nv) {
+      const uint32_t w = ws.words[t][v][lane >> 3];
+      if (writer) {
+        if (ws.cv[v].flags & kViewNoChanged) {
+          ws.cv[v].bits[word] = w;
+        } else {
+          const uint32_t d = w ^ prevw[v];
+          if (d) ws.cv[v].bits[word] = w;
+          ws.cv[v].delta[word] = d;
         }
+      }
+      if (ws.cv[v].n_visible) {
+        const uint32_t cnt = __reduce_add_sync(0xffffffffu, writer ? (uint32_t)__popc(w) : 0u);
+        if (lane == 0 && cnt) atomicAdd(ws.cv[v].n_visible, cnt);
       }
     }
   }
-  __syncthreads();  // shared views / totals are reused by the next item
+}
+
+// One work item (up to kItemTiles tiles of 128 objects x one group of up to VPP views)
+// by one warp.  ws.sc and `vkey` cache the warp's current scene and staged view group
+// across items.
+template <int VPP, bool PF>
+__device__ __forceinline__ void warp_item(const CullLaunch& a, uint32_t item, WarpShared& ws,
+                                          uint32_t& vkey)
+{
+  const int lane = threadIdx.x & 31;
+  __syncwarp();  // the previous item's reads of the shared state are done
+  if ((uint64_t)(item - ws.sc.item_begin) >=
+      (uint64_t)((ws.sc.n_tiles + kItemTiles - 1) / kItemTiles) * ws.sc.n_vgroups) {
+    const CullScene* src = a.scenes ? a.scenes + find_scene(a.scenes, a.n_scenes, item) : &a.one_scene;
+    constexpr int kSceneWords = (int)(sizeof(CullScene) / 4);
+    if (lane < kSceneWords) reinterpret_cast<uint32_t*>(&ws.sc)[lane] = reinterpret_cast<const uint32_t*>(src)[lane];
+    __syncwarp();
+  }
+  const CullScene& sc = ws.sc;
+  const uint32_t local = item - sc.item_begin;
+  const uint32_t group = local / sc.n_vgroups;
+  const uint32_t vfirst = (local - group * sc.n_vgroups) * VPP;
+  const int nv = (int)min((uint32_t)VPP, sc.n_views - vfirst);
+  const uint32_t tile_first = group * kItemTiles;
+  const uint32_t n_t = min((uint32_t)kItemTiles, sc.n_tiles - tile_first);
+
+  // Stage the views (matrices and output pointers) and their prefilter planes in the
+  // warp's shared memory when the view group changes; consecutive items of one scene
+  // keep them.
+  const uint32_t key = sc.view_begin + vfirst;
+  if (key != vkey) {
+    constexpr int kViewWords = (int)(sizeof(CullView) / 4);
+    static_assert(sizeof(CullView) % 16 == 0, "CullView is staged as whole words");
+    const uint32_t* src = reinterpret_cast<const uint32_t*>(a.views ? a.views + key : &a.one_view);
+    for (int i = lane; i < nv * kViewWords; i += 32) reinterpret_cast<uint32_t*>(ws.cv)[i] = src[i];
+    __syncwarp();
+    if (PF && lane < nv) pf::make_planes(ws.cv[lane].vp, ws.pl[lane]);
+    __syncwarp();
+    vkey = key;
+  }
+
+  uint32_t qn = 0;
+  for (uint32_t t = 0; t < n_t; ++t)
+    qn = classify_tile<VPP, PF>(a, ws, sc, tile_first + t, t, tile_first, nv, qn, lane);
+  if (PF && qn) drain_queue(ws, sc, tile_first, qn, lane);
+  else __syncwarp();
+  for (uint32_t t = 0; t < n_t; ++t) finish_tile<VPP>(ws, tile_first + t, t, nv, lane);
 }
 
 template <int VPP, bool PF>
 __global__ void __launch_bounds__(kThreads, 3) cull_kernel(const __grid_constant__ CullLaunch a)
 {
-  __shared__ CullShared sh;
+  __shared__ WarpShared wsh[kThreads / 32];
+  WarpShared& ws = wsh[threadIdx.x >> 5];
+  const int lane = threadIdx.x & 31;
   CullControl* ctl = a.ctl;
-  for (;;) {
-    if (threadIdx.x == 0) sh.item = atomicAdd(&ctl->ticket, a.items_per_ticket);
-    __syncthreads();
-    const uint32_t first = sh.item;
-    __syncthreads();
-    if (first >= a.n_items) break;
-    const uint32_t last = min(first + a.items_per_ticket, a.n_items);
-    for (uint32_t item = first; item < last; ++item) process_item<VPP, PF>(a, item, sh);
+  if (threadIdx.x % 32 == 0) {
+    ws.sc.item_begin = 0;  // no scene cached: the first item looks its scene up
+    ws.sc.n_tiles = 0;
+    ws.sc.n_vgroups = 1;
   }
+  uint32_t vkey = ~0u;
+  // Each warp claims its own tickets; the next claim is issued before the current items
+  // are processed, so its round trip overlaps them.
+  uint32_t first = 0;
+  if (lane == 0) first = atomicAdd(&ctl->ticket, a.items_per_ticket);
+  first = __shfl_sync(0xffffffffu, first, 0);
+  while (first < a.n_items) {
+    uint32_t next = 0;
+    if (lane == 0) next = atomicAdd(&ctl->ticket, a.items_per_ticket);
+    const uint32_t last = min(first + a.items_per_ticket, a.n_items);
+    for (uint32_t item = first; item < last; ++item) warp_item<VPP, PF>(a, item, ws, vkey);
+    first = __shfl_sync(0xffffffffu, next, 0);
+  }
+  __syncthreads();
   if (threadIdx.x == 0) {
     __threadfence();
     const unsigned int prev = atomicAdd(&ctl->done, 1u);
@@ -324,80 +379,97 @@ __global__ void __launch_bounds__(kThreads, 3) cull_kernel(const __grid_constant
 }
 
 // ---- changed-list assembly ----------------------------------------------------------------
-constexpr int kScanThreads = 1024;
+// The delta words are grouped in chunks of kDeltaChunk (one block, 16 words per thread).
+// delta_totals_kernel counts each chunk's changed objects; emit_changed_kernel adds the
+// earlier chunks' counts and writes every changed index, ascending.  No block waits on
+// another.
+constexpr int kScanThreads = 256;
+constexpr int kWordsPerThread = kDeltaChunk / kScanThreads;
+static_assert(kWordsPerThread % 4 == 0, "whole uint4 loads");
 
-// One CTA per view: exclusive scan of the tile counts into offsets, total into n_changed.
-__global__ void __launch_bounds__(kScanThreads)
-    scan_counts_kernel(const CullView* views, const __grid_constant__ CullView one)
+// The thread's delta words (n_words is a multiple of 4, the arrays 16-byte aligned).
+__device__ __forceinline__ void load_delta(const CullView& v, uint32_t b, uint32_t (&w)[kWordsPerThread])
 {
-  __shared__ uint32_t warp_sum[kScanThreads / 32];
-  const CullView& v = views ? views[blockIdx.x] : one;
-  const uint32_t n = v.n_tiles;
-  const uint32_t per = (n + kScanThreads - 1) / kScanThreads;
-  const uint32_t b = min(n, threadIdx.x * per), e = min(n, b + per);
-  // Independent loads, 8 in flight per thread (the counts were just written by the cull).
-  uint32_t s = 0;
-  for (uint32_t i = b; i < e; i += 8) {
-    uint32_t c[8];
 #pragma unroll
-    for (int j = 0; j < 8; ++j) c[j] = i + j < e ? __ldcg(v.counts + i + j) : 0u;
-#pragma unroll
-    for (int j = 0; j < 8; ++j) s += c[j];
+  for (int j = 0; j < kWordsPerThread; j += 4) {
+    uint4 q = make_uint4(0u, 0u, 0u, 0u);
+    if (b + j < v.n_words) q = __ldcg(reinterpret_cast<const uint4*>(v.delta + b + j));
+    w[j] = q.x;
+    w[j + 1] = q.y;
+    w[j + 2] = q.z;
+    w[j + 3] = q.w;
   }
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  uint32_t x = s;
-#pragma unroll
-  for (int d = 1; d < 32; d <<= 1) {
-    const uint32_t y = __shfl_up_sync(0xffffffffu, x, d);
-    if (lane >= d) x += y;
-  }
-  if (lane == 31) warp_sum[warp] = x;
-  __syncthreads();
-  if (warp == 0) {
-    uint32_t w = warp_sum[lane];
-#pragma unroll
-    for (int d = 1; d < 32; d <<= 1) {
-      const uint32_t y = __shfl_up_sync(0xffffffffu, w, d);
-      if (lane >= d) w += y;
-    }
-    warp_sum[lane] = w;  // inclusive over warps
-  }
-  __syncthreads();
-  uint32_t run = (warp ? warp_sum[warp - 1] : 0u) + x - s;
-  for (uint32_t i = b; i < e; i += 8) {
-    uint32_t c[8];
-#pragma unroll
-    for (int j = 0; j < 8; ++j) c[j] = i + j < e ? __ldcg(v.counts + i + j) : 0u;
-#pragma unroll
-    for (int j = 0; j < 8; ++j)
-      if (i + j < e) {
-        v.offsets[i + j] = run;
-        run += c[j];
-      }
-  }
-  if (threadIdx.x == kScanThreads - 1) *v.n_changed = warp_sum[31];
 }
 
-// blockIdx.y = view.  Each warp reads the counts and offsets of 32 consecutive tiles in
-// one coalesced load, then copies the slot ranges of the non-empty ones, all lanes per
-// tile, to their packed positions.
-__global__ void gather_changed_kernel(const CullView* views, const __grid_constant__ CullView one)
+// Block-wide exclusive scan of one value per thread; the block total goes to *total.
+__device__ __forceinline__ uint32_t block_scan(uint32_t x, uint32_t* wsum, uint32_t* total)
 {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const uint32_t incl = warp_scan(x, lane);
+  if (lane == 31) wsum[warp] = incl;
+  __syncthreads();
+  if (warp == 0) {
+    const uint32_t w = lane < kScanThreads / 32 ? wsum[lane] : 0u;
+    const uint32_t wi = warp_scan(w, lane);
+    if (lane < kScanThreads / 32) wsum[lane] = wi - w;
+    if (lane == 31) *total = wi;
+  }
+  __syncthreads();
+  return wsum[warp] + incl - x;
+}
+
+// grid = (chunks, views)
+__global__ void __launch_bounds__(kScanThreads)
+    delta_totals_kernel(const CullView* views, const __grid_constant__ CullView one)
+{
+  __shared__ uint32_t wsum[kScanThreads / 32];
+  __shared__ uint32_t tot;
   const CullView& v = views ? views[blockIdx.y] : one;
-  const int lane = threadIdx.x & 31;
-  const uint32_t warps = blockDim.x / 32;
-  for (uint32_t t0 = (blockIdx.x * warps + threadIdx.x / 32) * 32; t0 < v.n_tiles;
-       t0 += gridDim.x * warps * 32) {
-    const uint32_t t = t0 + lane;
-    const uint32_t c = t < v.n_tiles ? __ldcg(v.counts + t) : 0u;
-    const uint32_t o = t < v.n_tiles ? __ldcg(v.offsets + t) : 0u;
-    uint32_t busy = __ballot_sync(0xffffffffu, c != 0);
-    while (busy) {
-      const int k = __ffs(busy) - 1;
-      busy &= busy - 1u;
-      const uint32_t ck = __shfl_sync(0xffffffffu, c, k), ok = __shfl_sync(0xffffffffu, o, k);
-      const uint32_t* src = v.slots + (size_t)(t0 + k) * kTileObjects;
-      for (uint32_t j = lane; j < ck; j += 32) v.changed[ok + j] = __ldcg(src + j);
+  if ((v.flags & kViewNoChanged) || blockIdx.x * kDeltaChunk >= v.n_words) return;  // uniform
+  uint32_t w[kWordsPerThread];
+  load_delta(v, blockIdx.x * kDeltaChunk + threadIdx.x * kWordsPerThread, w);
+  uint32_t s = 0;
+#pragma unroll
+  for (int j = 0; j < kWordsPerThread; ++j) s += (uint32_t)__popc(w[j]);
+  block_scan(s, wsum, &tot);
+  if (threadIdx.x == 0) v.chunk_tot[blockIdx.x] = tot;
+}
+
+// grid = (chunks, views)
+__global__ void __launch_bounds__(kScanThreads)
+    emit_changed_kernel(const CullView* views, const __grid_constant__ CullView one)
+{
+  __shared__ uint32_t wsum[kScanThreads / 32];
+  __shared__ uint32_t tot;
+  const CullView& v = views ? views[blockIdx.y] : one;
+  if (v.flags & kViewNoChanged) return;  // uniform
+  const uint32_t w0 = blockIdx.x * kDeltaChunk;
+  if (w0 >= v.n_words) {  // uniform
+    if (blockIdx.x == 0 && threadIdx.x == 0) *v.n_changed = 0;
+    return;
+  }
+  // Changed objects of the earlier chunks.
+  const uint32_t n_chunks = (uint32_t)chunks_of(v.n_words);
+  uint32_t before = 0;
+  for (uint32_t i = threadIdx.x; i < blockIdx.x; i += kScanThreads) before += __ldcg(v.chunk_tot + i);
+  block_scan(before, wsum, &tot);
+  const uint32_t base = tot;
+  if (threadIdx.x == 0 && blockIdx.x == n_chunks - 1) *v.n_changed = base + __ldcg(v.chunk_tot + blockIdx.x);
+  __syncthreads();  // tot is reused below
+  const uint32_t b = w0 + threadIdx.x * kWordsPerThread;
+  uint32_t w[kWordsPerThread];
+  load_delta(v, b, w);
+  uint32_t s = 0;
+#pragma unroll
+  for (int j = 0; j < kWordsPerThread; ++j) s += (uint32_t)__popc(w[j]);
+  uint32_t pos = base + block_scan(s, wsum, &tot);
+#pragma unroll
+  for (int j = 0; j < kWordsPerThread; ++j) {
+    uint32_t m = w[j];
+    while (m) {
+      const int k = __ffs(m) - 1;
+      v.changed[pos++] = (b + (uint32_t)j) * 32u + (uint32_t)k;
+      m &= m - 1u;
     }
   }
 }
@@ -465,16 +537,13 @@ int cull_max_ctas_per_sm(int vpp)
 }
 
 int launch_changed_lists(const CullView* views, const CullView& one, uint32_t n_views,
-                         uint32_t max_tiles, void* stream)
+                         uint32_t max_words, void* stream)
 {
   cudaStream_t s = static_cast<cudaStream_t>(stream);
   if (!n_views) return 0;
-  scan_counts_kernel<<<n_views, kScanThreads, 0, s>>>(views, one);
-  const uint32_t warps = 8, tiles_per_cta = warps * 32;
-  uint32_t gx = (max_tiles + tiles_per_cta - 1) / tiles_per_cta;
-  if (gx > 1024) gx = 1024;
-  if (gx < 1) gx = 1;
-  gather_changed_kernel<<<dim3(gx, n_views), warps * 32, 0, s>>>(views, one);
+  const uint32_t chunks = std::max<uint32_t>(1, (uint32_t)chunks_of(max_words));
+  delta_totals_kernel<<<dim3(chunks, n_views), kScanThreads, 0, s>>>(views, one);
+  emit_changed_kernel<<<dim3(chunks, n_views), kScanThreads, 0, s>>>(views, one);
   return cudaGetLastError() == cudaSuccess ? 0 : -1;
 }
 

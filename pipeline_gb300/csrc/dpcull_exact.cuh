@@ -116,156 +116,4 @@ __device__ __forceinline__ bool obb_visible(const Obb& o, const float* vp)
   return acc.visible();
 }
 
-// ---------------------------------------------------------------------------------------
-// Conservative classification that never contradicts obb_visible().
-//
-// Let p, ex, ey, ez be the (float) box of make_obb and C_k = p + s ex + t ey + u ez the
-// 8 exact real corners; obb_visible() evaluates rounded corners c_k.  With col_j column j
-// of VP, the reference tests "lo a" (a = x, y, z) as c_a <= -c_w, i.e. c_a + c_w <= 0,
-// and "hi a" as !(c_a <= -c_w) && c_w <= c_a.  Let Pi = col_a + col_w (lo) or
-// col_w - col_a (hi) and B_a[i] = |col_a[i]| + |col_w[i]|.
-//   * rounding: |(c_a + c_w) - (C_a + C_w)| <= 7u * sum_i a_i B_a[i] <= 7u * A * N_a,
-//     u = 2^-24, a_i = |p_i|+|ex_i|+|ey_i|+|ez_i|, A = ||a||, N_a = ||B_a|| (the 4-term
-//     dot products and the 3-add corner chain, then Cauchy-Schwarz); the same bound holds
-//     for the hi test's c_w - c_a;
-//   * extent: over the 8 corners, C.Pi lies within centre.Pi +- (Rxyz n + Rw m), centre =
-//     p + (ex+ey+ez)/2, Rxyz = (||ex_xyz||+||ey_xyz||+||ez_xyz||)/2,
-//     Rw = (|ex_w|+|ey_w|+|ez_w|)/2, n = ||Pi_xyz||, m = |Pi_w|, since
-//     |e.Pi| <= ||e_xyz|| ||Pi_xyz|| + |e_w| |Pi_w| (Rw = 0 for affine world matrices);
-//   * this test: L = fl(cc_a +- cc_w) with cc = fl(centre' . VP) (FMA chains, centre'
-//     rounded) is within 9u * A * N_a of centre.Pi.
-// So with T >= Rxyz n + Rw m + 16u A N_a: L <= -T proves every rounded corner outside
-// that plane; "lo" outside sets the cfa bit (invisible); "hi" outside together with
-// L_lo > T_lo (no corner satisfies the lo test) sets the hi bit (invisible); L > T for all
-// six planes proves every corner strictly inside (cf = 0: visible).  Anything else is
-// undecided and goes through obb_visible().
-// Slack: the margin uses delta = 2^-19 = 32u for 16u; n and m come from Pi rounded in
-// float (|fl(x+y)| >= |x+y| (1-u)) and, like every norm here, are inflated by 2^-18 and
-// taken as the (inflated) L1 norm when tiny, so squares never underflow; eta = 2^-120
-// absorbs subnormal rounding.  The bounds need finite values without overflow: a box with
-// A >= 2^50 or a view with a non-finite entry or a norm >= 2^50 gets NaN bounds, every
-// comparison fails and the pair is undecided (then |terms| <= A N_a < 2^100).
-constexpr float kPfDelta = 0x1p-19f;
-constexpr float kPfInflate = 1.0f + 0x1p-18f;
-constexpr float kPfEta = 0x1p-120f;
-constexpr float kPfLimit = 0x1p50f;
-constexpr float kPfTiny = 0x1p-60f;
-
-__device__ __forceinline__ float pf_nan() { return __int_as_float(0x7fffffff); }
-
-// Upper bound of the Euclidean norm of (x, y, z[, w]).
-__device__ __forceinline__ float bound_norm(float x, float y, float z, float w = 0.f)
-{
-  const float l1 = (fabsf(x) + fabsf(y) + fabsf(z) + fabsf(w)) * kPfInflate;
-  if (l1 < kPfTiny) return l1 * kPfInflate;
-  return sqrtf(fmaf(x, x, fmaf(y, y, fmaf(z, z, w * w)))) * kPfInflate;
-}
-
-struct PfObject {
-  float4 c;    // box centre
-  float rxyz;  // Rxyz (inflated)
-  float rw;    // Rw (inflated)
-  float da;    // delta * A (inflated), NaN when the bounds do not apply
-};
-
-__device__ __forceinline__ PfObject pf_object(const Obb& o)
-{
-  PfObject b;
-  b.c = make_float4(fmaf(0.5f, o.ez.x, fmaf(0.5f, o.ey.x, fmaf(0.5f, o.ex.x, o.p.x))),
-                    fmaf(0.5f, o.ez.y, fmaf(0.5f, o.ey.y, fmaf(0.5f, o.ex.y, o.p.y))),
-                    fmaf(0.5f, o.ez.z, fmaf(0.5f, o.ey.z, fmaf(0.5f, o.ex.z, o.p.z))),
-                    fmaf(0.5f, o.ez.w, fmaf(0.5f, o.ey.w, fmaf(0.5f, o.ex.w, o.p.w))));
-  const float A = bound_norm(fabsf(o.p.x) + fabsf(o.ex.x) + fabsf(o.ey.x) + fabsf(o.ez.x),
-                             fabsf(o.p.y) + fabsf(o.ex.y) + fabsf(o.ey.y) + fabsf(o.ez.y),
-                             fabsf(o.p.z) + fabsf(o.ex.z) + fabsf(o.ey.z) + fabsf(o.ez.z),
-                             fabsf(o.p.w) + fabsf(o.ex.w) + fabsf(o.ey.w) + fabsf(o.ez.w)) *
-                  kPfInflate;
-  b.rxyz = 0.5f * (bound_norm(o.ex.x, o.ex.y, o.ex.z) + bound_norm(o.ey.x, o.ey.y, o.ey.z) +
-                   bound_norm(o.ez.x, o.ez.y, o.ez.z)) * kPfInflate;
-  b.rw = 0.5f * (fabsf(o.ex.w) + fabsf(o.ey.w) + fabsf(o.ez.w)) * kPfInflate * kPfInflate;
-  b.da = A < kPfLimit ? kPfDelta * A : pf_nan();
-  return b;
-}
-
-// Per-view bounds: N[a] for the rounding margin, and per plane (lo x, hi x, lo y, hi y,
-// lo z, hi z) the pair (n, m) of the extent term.  NaN when the view cannot be bounded.
-struct PfView {
-  float4 N;       // N_x, N_y, N_z, unused
-  float4 nm[3];   // axis a: (n_lo, m_lo, n_hi, m_hi)
-};
-
-__device__ __forceinline__ PfView pf_view(const float* vp)
-{
-  PfView r;
-  bool ok = true;
-  float N[3];
-  float nm[3][4];
-#pragma unroll
-  for (int a = 0; a < 3; ++a) {
-    float B[4], lo[4], hi[4];
-#pragma unroll
-    for (int i = 0; i < 4; ++i) {
-      const float ca = vp[4 * i + a], cw = vp[4 * i + 3];
-      ok &= isfinite(ca) && isfinite(cw);
-      B[i] = fabsf(ca) + fabsf(cw);
-      lo[i] = ca + cw;
-      hi[i] = cw - ca;
-    }
-    N[a] = bound_norm(B[0], B[1], B[2], B[3]) * kPfInflate;
-    nm[a][0] = bound_norm(lo[0], lo[1], lo[2]) * kPfInflate;
-    nm[a][1] = fabsf(lo[3]) * kPfInflate * kPfInflate;
-    nm[a][2] = bound_norm(hi[0], hi[1], hi[2]) * kPfInflate;
-    nm[a][3] = fabsf(hi[3]) * kPfInflate * kPfInflate;
-    ok &= N[a] < kPfLimit;
-  }
-  const float q = ok ? 0.f : pf_nan();  // NaN poisons every threshold of this view
-  r.N = make_float4(N[0] + q, N[1] + q, N[2] + q, 0.f);
-#pragma unroll
-  for (int a = 0; a < 3; ++a)
-    r.nm[a] = make_float4(nm[a][0] + q, nm[a][1] + q, nm[a][2] + q, nm[a][3] + q);
-  return r;
-}
-
-enum : int { kPfInvisible = 0, kPfVisible = 1, kPfAmbiguous = 2 };
-
-// View data read from shared memory once per (view, 4 objects).
-struct PfViewRegs {
-  float4 r0, r1, r2, r3;
-  PfView b;
-};
-
-__device__ __forceinline__ PfViewRegs pf_load_view(const float* vp, const PfView& pv)
-{
-  PfViewRegs v;
-  v.r0 = *reinterpret_cast<const float4*>(vp + 0);
-  v.r1 = *reinterpret_cast<const float4*>(vp + 4);
-  v.r2 = *reinterpret_cast<const float4*>(vp + 8);
-  v.r3 = *reinterpret_cast<const float4*>(vp + 12);
-  v.b = pv;
-  return v;
-}
-
-__device__ __forceinline__ int pf_classify(const PfObject& b, const PfViewRegs& v)
-{
-  const float cx = fmaf(b.c.w, v.r3.x, fmaf(b.c.z, v.r2.x, fmaf(b.c.y, v.r1.x, b.c.x * v.r0.x)));
-  const float cy = fmaf(b.c.w, v.r3.y, fmaf(b.c.z, v.r2.y, fmaf(b.c.y, v.r1.y, b.c.x * v.r0.y)));
-  const float cz = fmaf(b.c.w, v.r3.z, fmaf(b.c.z, v.r2.z, fmaf(b.c.y, v.r1.z, b.c.x * v.r0.z)));
-  const float cw = fmaf(b.c.w, v.r3.w, fmaf(b.c.z, v.r2.w, fmaf(b.c.y, v.r1.w, b.c.x * v.r0.w)));
-  const float ex = fmaf(b.da, v.b.N.x, kPfEta), ey = fmaf(b.da, v.b.N.y, kPfEta),
-              ez = fmaf(b.da, v.b.N.z, kPfEta);
-  const float txl = fmaf(b.rxyz, v.b.nm[0].x, fmaf(b.rw, v.b.nm[0].y, ex));
-  const float txh = fmaf(b.rxyz, v.b.nm[0].z, fmaf(b.rw, v.b.nm[0].w, ex));
-  const float tyl = fmaf(b.rxyz, v.b.nm[1].x, fmaf(b.rw, v.b.nm[1].y, ey));
-  const float tyh = fmaf(b.rxyz, v.b.nm[1].z, fmaf(b.rw, v.b.nm[1].w, ey));
-  const float tzl = fmaf(b.rxyz, v.b.nm[2].x, fmaf(b.rw, v.b.nm[2].y, ez));
-  const float tzh = fmaf(b.rxyz, v.b.nm[2].z, fmaf(b.rw, v.b.nm[2].w, ez));
-  const float lox = cx + cw, hix = cw - cx;
-  const float loy = cy + cw, hiy = cw - cy;
-  const float loz = cz + cw, hiz = cw - cz;
-  const bool out = (lox <= -txl) | ((hix <= -txh) & (lox > txl)) | (loy <= -tyl) |
-                   ((hiy <= -tyh) & (loy > tyl)) | (loz <= -tzl) | ((hiz <= -tzh) & (loz > tzl));
-  const bool in = (lox > txl) & (hix > txh) & (loy > tyl) & (hiy > tyh) & (loz > tzl) & (hiz > tzh);
-  return out ? kPfInvisible : (in ? kPfVisible : kPfAmbiguous);
-}
-
 }  // namespace dpcull

@@ -7,10 +7,11 @@
 // load of a tile stays inside the allocation.  World matrices are Mat44f rows
 // (4 x float4, row-major, row-vector convention) gathered by transform index.
 // A result (one group x one view) owns its visibility bit array (bit i of word i/32 is
-// object i, the ResultBitSet layout), its changed-object list and its scratch: one
-// changed count per tile, the tiles' exclusive offsets, and a tile-private slot range of
-// kTileObjects indices per tile (the cull writes each tile's changed objects there; a
-// scan of the counts and a gather then build the packed ascending list).
+// object i, the ResultBitSet layout, padded to whole tiles), its changed-object list and
+// its scratch: the delta words (bit i set where object i changed; the cull writes every
+// word) and one changed count per chunk of kDeltaChunk delta words.  Two small kernels
+// turn the delta words into the packed ascending list.  A tile is the 128 objects of one
+// warp.
 #pragma once
 
 #include <cstddef>
@@ -18,14 +19,33 @@
 
 struct dpcull_ctx_s;
 
+#if defined(__CUDACC__)
+#define DPCULL_HD_CONST __host__ __device__ constexpr
+#else
+#define DPCULL_HD_CONST constexpr
+#endif
+
 namespace dpcull {
 
-constexpr int kThreads = 256;                      // threads per CTA
+constexpr int kThreads = 256;                      // threads per CTA (8 independent warps)
+constexpr int kWarpsPerCta = kThreads / 32;
 constexpr int kObjPerThread = 4;                   // one float4 of each SoA row
-constexpr int kTileObjects = kThreads * kObjPerThread;  // 1024 objects per tile
-constexpr int kTileWords = kTileObjects / 32;      // 32 bit-array words per tile and view
+constexpr int kTileObjects = 32 * kObjPerThread;   // 128 objects per tile (one warp)
+constexpr int kTileWords = kTileObjects / 32;      // 4 bit-array words per tile and view
+constexpr int kItemTiles = 4;                      // tiles per work item (one warp, one view group)
+constexpr int kQueueCap = 1024;                    // undecided pairs a warp holds before a drain
+constexpr uint32_t kDeltaChunk = 4096;             // delta words per changed-list chunk
+
+// Work items of a scene: groups of kItemTiles tiles x view groups.
+DPCULL_HD_CONST uint32_t items_of(uint32_t n_tiles, uint32_t n_vgroups)
+{
+  return (n_tiles + kItemTiles - 1) / kItemTiles * n_vgroups;
+}
 constexpr int kMaxViewsPerPass = 8;                // views evaluated per object load
 constexpr uint32_t kMaxObjects = (1u << 30) - 1;   // keeps every index and count in 32 bits
+
+// Chunk counts of a view with n_words visibility words.
+DPCULL_HD_CONST size_t chunks_of(size_t n_words) { return (n_words + kDeltaChunk - 1) / kDeltaChunk; }
 
 // Error bits reported through CullControl::error.
 constexpr uint32_t kErrBadTransform = 1u;   // transform index >= matrix count
@@ -40,7 +60,7 @@ struct CullScene {
   uint32_t n_views;
   uint32_t n_vgroups;      // ceil(n_views / views per pass)
   uint32_t n_tiles;
-  uint32_t item_begin;     // first work item of this scene (items = tiles x view groups)
+  uint32_t item_begin;     // first work item of this scene (items_of(n_tiles, n_vgroups))
 };
 
 struct alignas(16) CullView {   // 128 bytes; staged whole into shared memory by the cull
@@ -48,16 +68,16 @@ struct alignas(16) CullView {   // 128 bytes; staged whole into shared memory by
   uint32_t* bits;        // previous visibility on entry, new visibility on exit
   uint32_t* changed;     // ascending changed-object list
   uint32_t* n_changed;   // its length
-  uint32_t* slots;       // scratch: kTileObjects changed indices per tile
-  uint32_t* counts;      // scratch: changed objects per tile
-  uint32_t* offsets;     // scratch: exclusive prefix of counts
-  uint32_t n_tiles;
+  uint32_t* delta;       // scratch: old XOR new visibility, n_words words
+  uint32_t* chunk_tot;   // scratch: changed objects per chunk of kDeltaChunk delta words
+  uint32_t n_words;      // visibility words of the view (whole tiles)
   uint32_t flags;        // kViewNoChanged: write the visibility words only
   uint32_t* n_visible;   // optional: number of visible objects (accumulated)
 };
+static_assert(sizeof(CullView) == 128, "CullView is 128 bytes");
 
 // CullView::flags: no previous visibility and no changed list (bits are overwritten;
-// changed / n_changed / slots / counts / offsets are not used).
+// changed / n_changed / delta / chunk_tot are not used).
 constexpr uint32_t kViewNoChanged = 1u;
 
 struct CullControl {
@@ -72,7 +92,7 @@ struct CullLaunch {
   const CullView* views;     // device array, or nullptr to use `one_view`
   uint32_t n_scenes;
   uint32_t n_items;
-  uint32_t items_per_ticket; // tiles claimed per ticket ("tiles per CTA" tuning knob)
+  uint32_t items_per_ticket; // items a warp claims per ticket (the "tiles per ticket" knob)
   uint32_t exact_only;       // 1 = skip the conservative prefilter (every pair exact)
   CullControl* ctl;
   CullScene one_scene;
@@ -83,10 +103,11 @@ struct CullLaunch {
 int launch_cull(const CullLaunch& args, int grid, int vpp, void* stream);
 int cull_max_ctas_per_sm(int vpp);
 // Changed-list assembly after a cull launch over `n_views` views (device array `views`,
-// or the single `one` when views is null): per-view scan of the tile counts, then the
-// gather of every tile's slots into the packed list.  max_tiles bounds n_tiles.
+// or the single `one` when views is null): per-chunk counts of the delta words, then the
+// emission of every changed index into the packed ascending list.  max_words bounds
+// n_words.
 int launch_changed_lists(const CullView* views, const CullView& one, uint32_t n_views,
-                         uint32_t max_tiles, void* stream);
+                         uint32_t max_words, void* stream);
 
 // Transform propagation (xform.cu).
 struct XformLaunch {

@@ -1,0 +1,238 @@
+// dpcull_prefilter.h -- conservative frustum classification that never contradicts the
+// reference's rounded box test (dp/culling/cpu/src/ManagerImpl.cpp:199-229,263-289).
+//
+// The cull decides most (object, view) pairs here, with a few FMA-pipe operations and
+// min/max, and sends only the pairs this test cannot decide through the exact test in the
+// reference's operation order (dpcull_exact.cuh).  Plain C++ on float: the same source is
+// compiled into the CUDA kernels and into a host test that checks it against the oracle.
+//
+// Notation.  The reference's cached box is the float 4-vectors p = (lower,1)*M and
+// X = ex*M_0, Y = ey*M_1, Z = ez*M_2 (M_i = row i of the world matrix).  Its 8 real
+// corners are C_s = p + s1 X + s2 Y + s3 Z; the reference evaluates rounded corners c_s =
+// fl(p*VP) + fl(X*VP) + ... (its add chain).  For an axis a in {x, y, z} with VP column
+// col_a and col_w, the reference's "lo" test on a corner is c_a <= -c_w, i.e.
+// c_a + c_w <= 0, and its "hi" test is !(c_a + c_w <= 0) && c_w - c_a <= 0.  A cfa bit
+// (ManagerImpl.cpp:224-227) is set when every corner has it; visible <=> no cfa bit.
+// u = 2^-24.
+//
+// Planes (per view).  Pi_lo = col_a + col_w, Pi_hi = col_w - col_a, B_a[i] = |col_a[i]| +
+// |col_w[i]| (so |Pi_i| <= B_a[i]), Nx_a = ||B_a,xyz||, Bw_a = B_a[w].  The stored plane
+// is Q = fl(fl(Pi) * r), r = fl(1 / Nx'_a) with Nx'_a >= Nx_a; hence Q = r Pi + eps,
+// |eps_i| <= 2.01u r |Pi_i|, r Nx_a <= 1 + u and ||Q_xyz|| <= 1 + 3.1u.  Stored with it:
+// q >= ||Q_xyz||, m >= |Q_w| and, per view, rho >= max_a Bw_a / Nx'_a.
+//
+// Box (per object).  b_j = sum_i (|l_i| + |e_i|) |M_ij| + |M_3j| bounds every magnitude
+// involved (|p_j| + |X_j| + |Y_j| + |Z_j| <= (1 + 5.01u) b_j); Bxyz >= ||b_xyz||,
+// bw >= b_w (bw = 1 for affine matrices).  For every axis, with S_a = sum_j b_j B_a[j]:
+// r S_a <= r (Bxyz Nx_a + bw Bw_a) <= (1 + u) Bxyz + bw rho (Cauchy-Schwarz on xyz only:
+// the view's translation row lives in w, apart from the objects' xyz magnitudes).
+// The centre K = p + (X + Y + Z) / 2 is the mean of the 8 corners.  We compute
+// c~ = (l + e/2) * M with FMAs: |c~_j - K_j| <= 9.7u b_j.  R >= (||X_xyz|| + ||Y_xyz|| +
+// ||Z_xyz||) / 2 and Rw >= (|X_w| + |Y_w| + |Z_w|) / 2, so for every corner C_s.Q lies in
+// K.Q +- E with E = R q + Rw m (|X.Q| <= ||X_xyz|| ||Q_xyz|| + |X_w| |Q_w|).
+//
+// Errors, in the plane's units (all of the form u r S_a):
+//   |r (c_a + c_w)_s - r C_s.Pi| <= 7.04u r S_a   (the reference's dot products and add
+//                                                  chain, 7u sum_j a_j B_a[j]),
+//   |C_s.eps| <= 2.02u r S_a,
+//   |L - K.Q| <= 13.75u r S_a   (L = fl(c~.Q), an FMA chain: 9.72u + 4.02u),
+// so every r (c_a + c_w)_s (and the hi analogue c_w - c_a) is within 22.9u (Bxyz + bw rho)
+// of the real value that L and E describe.  The margin is D = delta (Bxyz + bw rho) + eta
+// with delta = 2^-19 = 32u, which also absorbs the one rounding of t = fl(L + E) and
+// s = fl(L - E) (a relative u of the tested quantity); eta = 2^-120 absorbs subnormal
+// rounding.
+//
+// Decisions (for one view):
+//   * visible   if L > D for all six planes: the corner mean K is inside every plane, so
+//     for each plane some corner has a strictly positive rounded value and no cfa bit can
+//     be set;
+//   * invisible if for some axis t_lo = fl(L_lo + E_lo) <= -D (every corner passes the lo
+//     test), or t_hi <= -D and s_lo = fl(L_lo - E_lo) >= D (every corner fails the lo
+//     test and passes the hi test);
+//   * otherwise undecided.
+// The bounds need finite values without overflow: a box whose Bxyz or bw is not below
+// 2^50 (or is NaN) gets D = NaN, and a view whose entries are not finite, whose Nx'_a is
+// not in [2^-60, 2^50) or whose rho is not below 2^50 is marked not usable; every pair of
+// either is undecided.
+#pragma once
+
+#include <cmath>
+#include <cstdint>
+#include <cstring>
+
+#if defined(__CUDACC__)
+#define DPCULL_HD __host__ __device__ __forceinline__
+#else
+#define DPCULL_HD inline
+#endif
+
+namespace dpcull {
+namespace pf {
+
+#ifdef DPCULL_PF_TEST_DELTA
+// Host tests only: a deliberately weakened margin, to show that the tests can see one.
+constexpr float kDelta = DPCULL_PF_TEST_DELTA;
+#else
+constexpr float kDelta = 0x1p-19f;
+#endif
+constexpr float kInflate = 1.0f + 0x1p-18f;
+#ifdef DPCULL_PF_TEST_DELTA
+constexpr float kEta = 0.f;
+#else
+constexpr float kEta = 0x1p-120f;
+#endif
+constexpr float kLimit = 0x1p50f;
+constexpr float kTiny = 0x1p-60f;
+
+struct alignas(16) F4 {
+  float x, y, z, w;
+};
+
+DPCULL_HD float nan_value()
+{
+  const uint32_t bits = 0x7fc00000u;
+  float f;
+  memcpy(&f, &bits, sizeof f);
+  return f;
+}
+
+// Upper bound of the Euclidean norm of (x, y, z, w): the inflated square root of the FMA
+// sum of squares, or the inflated L1 norm when the squares could underflow.
+DPCULL_HD float bound_norm(float x, float y, float z, float w = 0.f)
+{
+  const float l1 = (std::fabs(x) + std::fabs(y) + std::fabs(z) + std::fabs(w)) * kInflate;
+  if (l1 < kTiny) return l1 * kInflate;
+  return std::sqrt(std::fma(x, x, std::fma(y, y, std::fma(z, z, w * w)))) * kInflate;
+}
+
+// Prefilter planes of one view (160 bytes, staged in shared memory by the cull).
+struct Planes {
+  F4 q[3][2];  // axis a: lo plane Q_lo, hi plane Q_hi
+  F4 nm[3];    // axis a: (q_lo, q_hi, m_lo, m_hi)
+  F4 rho;      // (rho, 0, 0, 0); rho is NaN when the view cannot be bounded
+};
+
+// Builds the planes of a row-major Mat44f view-projection; false when the view cannot be
+// bounded (its pairs then all take the exact test).
+DPCULL_HD bool make_planes(const float* vp, Planes& out)
+{
+  bool ok = true;
+  for (int i = 0; i < 16; ++i) ok = ok && std::isfinite(vp[i]);
+  float rho = 0.f;
+  for (int a = 0; a < 3; ++a) {
+    float B[4], lo[4], hi[4];
+    for (int i = 0; i < 4; ++i) {
+      const float ca = vp[4 * i + a], cw = vp[4 * i + 3];
+      B[i] = std::fabs(ca) + std::fabs(cw);
+      lo[i] = ca + cw;
+      hi[i] = cw - ca;
+    }
+    const float nx = bound_norm(B[0], B[1], B[2]) * kInflate;
+    ok = ok && nx < kLimit && nx >= kTiny;
+    const float r = ok ? 1.0f / nx : 0.f;
+    rho = std::fmax(rho, B[3] * r * kInflate);
+    F4 ql = {lo[0] * r, lo[1] * r, lo[2] * r, lo[3] * r};
+    F4 qh = {hi[0] * r, hi[1] * r, hi[2] * r, hi[3] * r};
+    out.q[a][0] = ql;
+    out.q[a][1] = qh;
+    out.nm[a] = F4{bound_norm(ql.x, ql.y, ql.z) * kInflate, bound_norm(qh.x, qh.y, qh.z) * kInflate,
+                   std::fabs(ql.w) * kInflate, std::fabs(qh.w) * kInflate};
+  }
+  ok = ok && rho < kLimit;
+  // A NaN rho makes every margin of the view NaN: no comparison holds, nothing is decided.
+  out.rho = F4{ok ? rho : nan_value(), 0.f, 0.f, 0.f};
+  return ok;
+}
+
+// Prefilter box of one object: centre c (c.w == 1 for affine matrices), extent bounds R
+// and Rw, and the margin in two parts: d0 = delta Bxyz + eta (NaN when the bounds do not
+// apply) and dw = delta bw; a view's margin is D = dw rho + d0.
+struct Box {
+  float cx, cy, cz, cw;
+  float r, rw, d0, dw;
+};
+
+// Upper bound of ||(r.x, r.y, r.z)||: the 2^-120 addend keeps every partial sum normal.
+DPCULL_HD float row_norm(const F4& m)
+{
+  return std::sqrt(std::fma(m.x, m.x, std::fma(m.y, m.y, std::fma(m.z, m.z, 0x1p-120f)))) * kInflate;
+}
+
+// True when the matrix maps w = 1 to w = 1 and directions to w = 0 (no projective part):
+// then c.w == 1 exactly and Rw == 0.
+DPCULL_HD bool is_affine(const F4& m0, const F4& m1, const F4& m2, const F4& m3)
+{
+  return m0.w == 0.f && m1.w == 0.f && m2.w == 0.f && m3.w == 1.f;
+}
+
+DPCULL_HD Box make_box(float lx, float ly, float lz, float ex, float ey, float ez, const F4& m0,
+                       const F4& m1, const F4& m2, const F4& m3)
+{
+  const float cx0 = lx + 0.5f * ex, cy0 = ly + 0.5f * ey, cz0 = lz + 0.5f * ez;
+  Box b;
+  b.cx = std::fma(cz0, m2.x, std::fma(cy0, m1.x, std::fma(cx0, m0.x, m3.x)));
+  b.cy = std::fma(cz0, m2.y, std::fma(cy0, m1.y, std::fma(cx0, m0.y, m3.y)));
+  b.cz = std::fma(cz0, m2.z, std::fma(cy0, m1.z, std::fma(cx0, m0.z, m3.z)));
+  b.cw = std::fma(cz0, m2.w, std::fma(cy0, m1.w, std::fma(cx0, m0.w, m3.w)));
+  const float n0 = row_norm(m0), n1 = row_norm(m1), n2 = row_norm(m2);
+  const float aex = std::fabs(ex), aey = std::fabs(ey), aez = std::fabs(ez);
+  b.r = 0.5f * kInflate * (aex * n0 + aey * n1 + aez * n2);
+  b.rw = 0.5f * kInflate *
+         (aex * std::fabs(m0.w) + aey * std::fabs(m1.w) + aez * std::fabs(m2.w));
+  const float sx = std::fabs(lx) + aex, sy = std::fabs(ly) + aey, sz = std::fabs(lz) + aez;
+  const float bxyz = kInflate * (sx * n0 + sy * n1 + sz * n2 +
+                                 (std::fabs(m3.x) + std::fabs(m3.y) + std::fabs(m3.z)));
+  const float bw = kInflate * (sx * std::fabs(m0.w) + sy * std::fabs(m1.w) +
+                               sz * std::fabs(m2.w) + std::fabs(m3.w));
+  b.d0 = (bxyz < kLimit && bw < kLimit) ? std::fma(kDelta, bxyz, kEta) : nan_value();
+  b.dw = kDelta * bw;
+  return b;
+}
+
+// One axis of one view for one box: folds the axis's planes into the running minima
+//   mi = min over planes of L (the visible test), mo = min over axes of the invisible
+//   candidate min(t_lo, max(t_hi, -s_lo)).
+// kAffine: the box's matrix is affine (c.w == 1, Rw == 0).
+template <bool kAffine>
+DPCULL_HD void axis(const Box& b, const F4& ql, const F4& qh, const F4& nm, float& mi, float& mo)
+{
+  float Ll, Lh;
+  if (kAffine) {
+    // c.w == 1: Q_w is the addend; E = R q, and t = fl(L + R q), s = fl(L - R q) are one
+    // rounding each.
+    Ll = std::fma(b.cz, ql.z, std::fma(b.cy, ql.y, std::fma(b.cx, ql.x, ql.w)));
+    Lh = std::fma(b.cz, qh.z, std::fma(b.cy, qh.y, std::fma(b.cx, qh.x, qh.w)));
+    const float tl = std::fma(b.r, nm.x, Ll), sl = std::fma(-b.r, nm.x, Ll);
+    const float th = std::fma(b.r, nm.y, Lh);
+    mo = std::fmin(mo, std::fmin(tl, std::fmax(th, -sl)));
+  } else {
+    Ll = std::fma(b.cw, ql.w, std::fma(b.cz, ql.z, std::fma(b.cy, ql.y, b.cx * ql.x)));
+    Lh = std::fma(b.cw, qh.w, std::fma(b.cz, qh.z, std::fma(b.cy, qh.y, b.cx * qh.x)));
+    const float El = std::fma(b.rw, nm.z, b.r * nm.x), Eh = std::fma(b.rw, nm.w, b.r * nm.y);
+    const float tl = Ll + El, sl = Ll - El, th = Lh + Eh;
+    mo = std::fmin(mo, std::fmin(tl, std::fmax(th, -sl)));
+  }
+  mi = std::fmin(mi, std::fmin(Ll, Lh));
+}
+
+enum : int { kInvisible = 0, kVisible = 1, kUndecided = 2 };
+
+// Whole classification of one box in one view (the kernels inline the same steps, with
+// the view's planes shared by several boxes).
+DPCULL_HD int classify(const Box& b, const Planes& p, bool view_ok, bool affine)
+{
+  if (!view_ok) return kUndecided;
+  const float inf = INFINITY;
+  const float d = std::fma(b.dw, p.rho.x, b.d0);
+  float mi = inf, mo = inf;
+  for (int a = 0; a < 3; ++a) {
+    if (affine) axis<true>(b, p.q[a][0], p.q[a][1], p.nm[a], mi, mo);
+    else axis<false>(b, p.q[a][0], p.q[a][1], p.nm[a], mi, mo);
+  }
+  if (mi > d) return kVisible;
+  if (mo <= -d) return kInvisible;
+  return kUndecided;
+}
+
+}  // namespace pf
+}  // namespace dpcull

@@ -7,12 +7,12 @@
 // budget reserved up front) has none to give.  The regular entry points allocate their
 // result buffers and the cull's scratch lazily, so they are unusable there.  This entry
 // point runs the same cull kernel and the same changed-list kernels on buffers the
-// caller owns, and takes its scratch (per-tile changed counts, their offsets, the
-// per-tile index slots and the work-ticket word) from one statically sized device
-// array defined below.  It calls no cudaMalloc, cudaFree or other allocating routine.
+// caller owns, and takes its scratch (the delta words of the changed list, their
+// per-chunk counts and the work-ticket word) from one statically sized device array
+// defined below.  It calls no cudaMalloc, cudaFree or other allocating routine.
 //
 // The array lives in every GPU that loads this library until the process exits
-// (about 4 MB).  Its device address is looked up once per device, with that device
+// (about 128 KB).  Its device address is looked up once per device, with that device
 // current, on the first call made on the device; make that first call before any
 // stream capture.  All calls share the array and it keeps the last call's contents:
 // each call clears the parts that must start at zero, and calls whose work overlaps on
@@ -30,13 +30,14 @@
 namespace dpcull {
 namespace {
 
-constexpr size_t kNoallocTiles = DPCULL_NOALLOC_MAX_OBJECTS / kTileObjects;
-constexpr size_t kSlotsBytes = kNoallocTiles * kTileObjects * sizeof(uint32_t);
-constexpr size_t kCountsBytes = kNoallocTiles * sizeof(uint32_t);
-constexpr size_t kCtlOffset = kSlotsBytes + 2 * kCountsBytes;
+constexpr size_t kNoallocWords = DPCULL_NOALLOC_MAX_OBJECTS / 32;
+constexpr size_t kDeltaBytes = kNoallocWords * sizeof(uint32_t);
+constexpr size_t kChunkOffset = kDeltaBytes;
+constexpr size_t kCtlOffset = kChunkOffset + (chunks_of(kNoallocWords) * sizeof(uint32_t) + 255) / 256 * 256;
 constexpr size_t kScratchBytes = kCtlOffset + 256;
+static_assert(DPCULL_NOALLOC_MAX_OBJECTS % kTileObjects == 0, "whole tiles");
 
-// The scratch: slots | counts | offsets | control block.
+// The scratch: delta words | chunk counts | control block.
 static __device__ __align__(256) unsigned char g_scratch[kScratchBytes];
 
 constexpr int kMaxDevices = 64;
@@ -118,12 +119,12 @@ extern "C" int dpcull_cull_noalloc(const float* objects, size_t cap, size_t n, c
   a.one_view.bits = bits;
   a.one_view.changed = changed;
   a.one_view.n_changed = n_changed;
-  a.one_view.slots = reinterpret_cast<uint32_t*>(s);
-  a.one_view.counts = reinterpret_cast<uint32_t*>(s + kSlotsBytes);
-  a.one_view.offsets = reinterpret_cast<uint32_t*>(s + kSlotsBytes + kCountsBytes);
-  a.one_view.n_tiles = tiles;
-  a.n_items = tiles;
-  if (launch_cull(a, (int)tiles, 1, st) || launch_changed_lists(nullptr, a.one_view, 1, tiles, st)) {
+  a.one_view.delta = reinterpret_cast<uint32_t*>(s);
+  a.one_view.chunk_tot = reinterpret_cast<uint32_t*>(s + kChunkOffset);
+  a.one_view.n_words = tiles * kTileWords;
+  a.n_items = items_of(tiles, 1);
+  const int grid = (int)((a.n_items + kWarpsPerCta - 1) / kWarpsPerCta);  // one item per warp
+  if (launch_cull(a, grid, 1, st) || launch_changed_lists(nullptr, a.one_view, 1, a.one_view.n_words, st)) {
     cudaGetLastError();
     return noalloc_fail(DPCULL_ERR_CUDA, "dpcull_cull_noalloc: launch failed");
   }

@@ -310,7 +310,7 @@ bool launch(dpcull_server s, Slot& slot)
     cs.n_vgroups = (q.n_views + vpp - 1) / vpp;
     cs.n_tiles = (uint32_t)(sc.cap / kTileObjects);
     cs.item_begin = items;
-    items += cs.n_tiles * cs.n_vgroups;
+    items += items_of(cs.n_tiles, cs.n_vgroups);
     max_tiles = std::max(max_tiles, cs.n_tiles);
     slot.h_scenes[i] = cs;
     slot.bits_off.push_back(words_off);
@@ -320,7 +320,7 @@ bool launch(dpcull_server s, Slot& slot)
       cv.bits = slot.d_out + words_off + v * (sc.cap / 32);
       cv.flags = kViewNoChanged;
       cv.n_visible = counts + vi;
-      cv.n_tiles = cs.n_tiles;
+      cv.n_words = cs.n_tiles * kTileWords;
       slot.h_views[vi] = cv;
     }
     if (q.flags & DPCULL_REQUEST_KEEP_BITS) {
@@ -339,7 +339,8 @@ bool launch(dpcull_server s, Slot& slot)
   a.items_per_ticket = 1;
   a.ctl = slot.ctl;
   const int occ = cull_max_ctas_per_sm(vpp);
-  const int grid = (int)std::max<long long>(1, std::min<long long>((long long)s->sm_count * occ, items));
+  const long long want = ((long long)items + kWarpsPerCta - 1) / kWarpsPerCta;  // a warp per item
+  const int grid = (int)std::max<long long>(1, std::min<long long>((long long)s->sm_count * occ, want));
   launch_cull(a, grid, vpp, slot.stream);
   cudaMemcpyAsync(slot.h_counts, counts, n_views * 4, cudaMemcpyDeviceToHost, slot.stream);
   if (kept_words) {

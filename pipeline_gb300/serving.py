@@ -40,7 +40,7 @@ def make_templates(seed: int, n_templates: int, nmin: float = 1e4, nmax: float =
 
 
 def scene_bytes(n: int, n_mats: int) -> int:
-    cap = -(-n // 1024) * 1024
+    cap = -(-n // 128) * 128
     return 7 * cap * 4 + 64 * n_mats
 
 

@@ -1,0 +1,195 @@
+"""The cull's conservative prefilter (pipeline_gb300/csrc/dpcull_prefilter.h), compiled for
+the host from the same source as the kernels, against the oracle's exact visibility
+(dp/culling/cpu/src/ManagerImpl.cpp:263-289): wherever the prefilter decides a pair, the
+decision must equal the reference's rounded result.  Families: the benchmark
+distributions under cube, stereo, cascade and random perspective views; boxes centred on
+the frustum planes at every scale; projective world matrices; extreme coordinates and
+clip ranges; non-finite values.  A build with a deliberately weakened margin must
+disagree somewhere, which shows that the families reach the rounding boundary."""
+import ctypes
+import subprocess
+
+import numpy as np
+import pytest
+
+import oracle
+from conftest import ROOT
+from pipeline_gb300 import workloads as wl
+
+
+def _build(tmp_path, name, extra=()):
+    so = tmp_path / f"{name}.so"
+    cmd = ["g++", "-std=c++17", "-O2", "-ffp-contract=off", "-shared", "-fPIC", *extra,
+           "-I", str(ROOT / "pipeline_gb300" / "csrc"), str(ROOT / "tests" / "cpp" / "prefilter_host.cpp"),
+           "-o", str(so)]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    lib = ctypes.CDLL(str(so))
+    lib.pf_classify_soa.argtypes = [ctypes.c_size_t] + [ctypes.c_void_p] * 6
+    lib.pf_classify_soa.restype = None
+    return lib
+
+
+@pytest.fixture(scope="module")
+def pf(tmp_path_factory):
+    return _build(tmp_path_factory.mktemp("pf"), "pf")
+
+
+@pytest.fixture(scope="module")
+def pf_weak(tmp_path_factory):
+    return _build(tmp_path_factory.mktemp("pfw"), "pfw", ["-DDPCULL_PF_TEST_DELTA=0.0f"])
+
+
+def classify(lib, lower, extent, xform, mats, vp):
+    n = lower.shape[1]
+    out = np.empty(n, np.int8)
+    args = [np.ascontiguousarray(a) for a in (lower, extent, xform, mats, np.asarray(vp, np.float32).reshape(16))]
+    lib.pf_classify_soa(n, *[a.ctypes.data for a in args], out.ctypes.data)
+    return out
+
+
+def exact(lower, extent, xform, mats, vp):
+    n = lower.shape[1]
+    bits = oracle.cull_bits(lower, extent, xform, mats, vp)
+    return ((bits[np.arange(n) >> 5] >> (np.arange(n) & 31).astype(np.uint32)) & 1).astype(bool)
+
+
+def check(lib, scene, vps):
+    """Returns (pairs, decided, wrong) over all views."""
+    pairs = decided = wrong = 0
+    for vp in vps:
+        cls = classify(lib, *scene, vp)
+        ex = exact(*scene, vp)
+        dec = cls != 2
+        wrong += int(np.count_nonzero(dec & ((cls == 1) != ex)))
+        pairs += cls.size
+        decided += int(np.count_nonzero(dec))
+    return pairs, decided, wrong
+
+
+def boxes_scene(rng, n, centres_world, extent_scale, affine=True):
+    """n boxes centred at the given world points: random rotation and scale, the box
+    translated so that its centre lands on the point."""
+    lower_c = np.zeros((3, n))
+    e = np.exp(rng.uniform(np.log(extent_scale[0]), np.log(extent_scale[1]), (3, n)))
+    lower = (lower_c - 0.5 * e).astype(np.float32)
+    extent = e.astype(np.float32)
+    mats = wl.random_matrices(rng, n).reshape(n, 4, 4).astype(np.float64)
+    mats[:, 3, :3] = centres_world
+    if not affine:
+        mats[:, :3, 3] = rng.normal(0, 1e-3, (n, 3))
+        mats[:, 3, 3] = rng.uniform(0.5, 2.0, n)
+    return (np.ascontiguousarray(lower), np.ascontiguousarray(extent),
+            np.arange(n, dtype=np.uint32), mats.reshape(n, 16).astype(np.float32))
+
+
+def points_on_planes(rng, vp, n, depth_range):
+    """World points on the six clip planes of vp (clip x, y or z equal to +-w)."""
+    inv = np.linalg.inv(np.asarray(vp, np.float64).reshape(4, 4))
+    w = np.exp(rng.uniform(np.log(depth_range[0]), np.log(depth_range[1]), n))
+    clip = np.empty((n, 4))
+    clip[:, 3] = w
+    clip[:, :3] = rng.uniform(-1, 1, (n, 3)) * w[:, None]
+    axis = rng.integers(0, 3, n)
+    sign = rng.choice([-1.0, 1.0], n)
+    clip[np.arange(n), axis] = sign * w
+    world = clip @ inv
+    return world[:, :3] / world[:, 3:4]
+
+
+def test_prefilter_benchmark_views(pf):
+    """The benchmark distributions (plain, stress) in every view family: never wrong, and
+    it decides nearly every pair."""
+    rng = np.random.default_rng(11)
+    n = 60_000
+    lower, _, extent = wl.random_boxes(rng, n)
+    mats = wl.random_matrices(rng, 4096)
+    xform = rng.integers(0, 4096, n).astype(np.uint32)
+    vps = (wl.cube_face_views() + wl.stereo_views() + wl.cascade_views()
+           + [wl.look_at(rng.uniform(-900, 900, 3), rng.uniform(-900, 900, 3), (0, 1, 0)) @ wl.perspective()
+              for _ in range(4)])
+    pairs, decided, wrong = check(pf, (lower, extent, xform, mats), vps)
+    assert wrong == 0
+    assert decided >= 0.98 * pairs, (decided, pairs)
+
+
+def test_prefilter_camera_inside_cloud(pf):
+    rng = np.random.default_rng(12)
+    n = 40_000
+    lower, _, extent = wl.random_boxes(rng, n)
+    mats = wl.random_matrices(rng, n).reshape(n, 4, 4)
+    mats[:, 3, :3] = rng.uniform(-20, 20, (n, 3))
+    mats = mats.reshape(n, 16)
+    scene = (lower, extent, np.arange(n, dtype=np.uint32), mats)
+    vps = wl.cube_face_views() + wl.stereo_views()
+    pairs, decided, wrong = check(pf, scene, vps)
+    assert wrong == 0
+    assert decided >= 0.6 * pairs  # boxes of 0.1-20 units within 35 units: many straddle
+
+
+@pytest.mark.parametrize("scale", [(1e-7, 1e-5), (1e-4, 1e-2), (0.1, 10.0)])
+def test_prefilter_boxes_on_planes(pf, scale):
+    """Boxes centred exactly on the frustum planes: the rounding decides many of them."""
+    rng = np.random.default_rng(13)
+    n = 30_000
+    vps = wl.cube_face_views() + wl.stereo_views()[:1] + wl.cascade_views()[:2]
+    for vp in vps:
+        pts = points_on_planes(rng, vp, n, (0.2, 4000.0))
+        for affine in (True, False):
+            scene = boxes_scene(rng, n, pts, scale, affine)
+            _, _, wrong = check(pf, scene, [vp])
+            assert wrong == 0
+
+
+def test_prefilter_extreme_ranges(pf):
+    """Large translations, tiny and huge clip ranges, tiny boxes."""
+    rng = np.random.default_rng(14)
+    n = 20_000
+    for trans, near, far in [(1e6, 0.1, 1e7), (1e3, 1e-5, 1e3), (1e2, 1.0, 1e9), (1e9, 1e3, 1e12)]:
+        P = wl.perspective(60.0, 16 / 9, near, far)
+        eye = rng.uniform(-trans, trans, 3)
+        vps = [wl.look_at(eye, eye + rng.normal(size=3), (0, 1, 0)) @ P for _ in range(3)]
+        for vp in vps:
+            pts = points_on_planes(rng, vp, n, (near * 1.5, far * 0.9))
+            for scale in [(1e-6 * trans, 1e-3 * trans), (1e-2, 1.0)]:
+                _, _, wrong = check(pf, boxes_scene(rng, n, pts, scale), [vp])
+                assert wrong == 0
+            # and boxes spread through the volume
+            pts = eye + rng.normal(0, trans, (n, 3))
+            _, _, wrong = check(pf, boxes_scene(rng, n, pts, (1e-3 * trans, trans)), [vp])
+            assert wrong == 0
+
+
+def test_prefilter_specials(pf):
+    """NaN, infinities, huge and subnormal values in boxes, matrices and views."""
+    rng = np.random.default_rng(15)
+    n = 20_000
+    lower, _, extent = wl.random_boxes(rng, n)
+    mats = wl.random_matrices(rng, n)
+    specials = np.array([np.nan, np.inf, -np.inf, 3e38, -3e38, 1e-40, -1e-40, 0.0, -0.0, 2e15],
+                        np.float32)
+    for arr in (lower, extent, mats):
+        flat = arr.reshape(-1)
+        k = rng.integers(0, flat.size, flat.size // 50)
+        flat[k] = rng.choice(specials, k.size)
+    scene = (lower, extent, np.arange(n, dtype=np.uint32), mats)
+    vps = [wl.perspective()] + wl.cube_face_views()[:2]
+    bad = np.asarray(wl.perspective(), np.float32).copy().reshape(16)
+    for v in specials:
+        b = bad.copy()
+        b[rng.integers(0, 16)] = v
+        vps.append(b)
+    _, _, wrong = check(pf, scene, vps)
+    assert wrong == 0
+
+
+def test_weak_margin_is_caught(pf_weak):
+    """With the margin removed, the boxes-on-planes family exposes disagreements: the
+    families above do reach the reference's rounding boundary."""
+    rng = np.random.default_rng(13)
+    n = 30_000
+    wrong = 0
+    for vp in wl.cube_face_views()[:3]:
+        pts = points_on_planes(rng, vp, n, (0.2, 4000.0))
+        wrong += check(pf_weak, boxes_scene(rng, n, pts, (1e-7, 1e-5)), [vp])[2]
+    assert wrong > 0
