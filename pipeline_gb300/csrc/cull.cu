@@ -90,7 +90,7 @@ __device__ __forceinline__ bool exact_visible(const CullScene& sc, uint32_t i, c
 
 // Prefilter of the lane's 4 boxes in each view of the item: visible objects into nib[v]
 // (bit k), undecided pairs into amb (bit 8k + v).  Branch-free per pair.
-template <int VPP, bool kAffine>
+template <int VPP>
 __device__ __forceinline__ void classify_views(const WarpShared& ws, const pf::Box (&bx)[kObjPerThread],
                                                int nv, uint32_t valid, uint32_t (&nib)[VPP],
                                                uint32_t& amb)
@@ -99,20 +99,22 @@ __device__ __forceinline__ void classify_views(const WarpShared& ws, const pf::B
   for (int v = 0; v < VPP; ++v) {
     if (v < nv) {
       const pf::Planes& P = ws.pl[v];
-      const float rho = P.rho.x;
+      const pf::F4 n01 = P.n01, n2g = P.n2g;
       float mi[kObjPerThread], mo[kObjPerThread];
 #pragma unroll
       for (int k = 0; k < kObjPerThread; ++k) mi[k] = mo[k] = __int_as_float(0x7f800000);
 #pragma unroll
       for (int ax = 0; ax < 3; ++ax) {
-        const pf::F4 ql = P.q[ax][0], qh = P.q[ax][1], nm = P.nm[ax];
+        const pf::F4 ql = P.q[ax][0], qh = P.q[ax][1];
+        const float nl = ax == 0 ? n01.x : ax == 1 ? n01.z : n2g.x;
+        const float nh = ax == 0 ? n01.y : ax == 1 ? n01.w : n2g.y;
 #pragma unroll
-        for (int k = 0; k < kObjPerThread; ++k) pf::axis<kAffine>(bx[k], ql, qh, nm, mi[k], mo[k]);
+        for (int k = 0; k < kObjPerThread; ++k) pf::axis(bx[k], ql, qh, nl, nh, mi[k], mo[k]);
       }
       uint32_t in = 0, und = 0;
 #pragma unroll
       for (int k = 0; k < kObjPerThread; ++k) {
-        const float d = fmaf(bx[k].dw, rho, bx[k].d0);
+        const float d = bx[k].d0 + n2g.z;
         const bool vis = mi[k] > d, out = mo[k] <= -d;
         in |= (uint32_t)vis << k;
         und |= (uint32_t)(!vis && !out) << k;
@@ -180,7 +182,6 @@ __device__ __forceinline__ uint32_t classify_tile(const CullLaunch& a, WarpShare
     // view's planes are read once for all 4 objects.
     pf::Box bx[kObjPerThread];
     uint32_t valid = 0;
-    bool affine = true;
 #pragma unroll
     for (int k = 0; k < kObjPerThread; ++k) {
       const uint32_t mi = compu(xf, k);
@@ -199,13 +200,9 @@ __device__ __forceinline__ uint32_t classify_tile(const CullLaunch& a, WarpShare
       const pf::F4 m2{r2.x, r2.y, r2.z, r2.w}, m3{r3.x, r3.y, r3.z, r3.w};
       bx[k] = pf::make_box(comp(lx, k), comp(ly, k), comp(lz, k), comp(ex, k), comp(ey, k),
                            comp(ez, k), m0, m1, m2, m3);
-      affine = affine && (!use || pf::is_affine(m0, m1, m2, m3));
       valid |= (uint32_t)use << k;
     }
-    // Affine world matrices (c.w == 1, no w extent) take the shorter plane test; the
-    // choice is uniform over the warp.
-    if (__all_sync(0xffffffffu, affine)) classify_views<VPP, true>(ws, bx, nv, valid, nib, amb);
-    else classify_views<VPP, false>(ws, bx, nv, valid, nib, amb);
+    classify_views<VPP>(ws, bx, nv, valid, nib, amb);
   } else {
 #pragma unroll
     for (int k = 0; k < kObjPerThread; ++k) {

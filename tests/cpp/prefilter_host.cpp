@@ -7,15 +7,6 @@
 
 using dpcull::pf::F4;
 
-extern "C" int pf_make_planes(const float* vp, float* planes36)
-{
-  dpcull::pf::Planes p;
-  const bool ok = dpcull::pf::make_planes(vp, p);
-  const float* src = &p.q[0][0].x;
-  for (int i = 0; i < 36; ++i) planes36[i] = src[i];
-  return ok ? 1 : 0;
-}
-
 // Classification of n objects (planar [3][n] lower / extent rows, transform indices into
 // mats[][16]) in one view: 0 invisible, 1 visible, 2 undecided.
 extern "C" void pf_classify_soa(size_t n, const float* lower, const float* extent,
@@ -23,7 +14,7 @@ extern "C" void pf_classify_soa(size_t n, const float* lower, const float* exten
                                 int8_t* out)
 {
   dpcull::pf::Planes p;
-  const bool ok = dpcull::pf::make_planes(vp, p);
+  dpcull::pf::make_planes(vp, p);
   for (size_t i = 0; i < n; ++i) {
     const float* m = mats + 16 * (size_t)idx[i];
     const F4 m0{m[0], m[1], m[2], m[3]}, m1{m[4], m[5], m[6], m[7]};
@@ -31,6 +22,6 @@ extern "C" void pf_classify_soa(size_t n, const float* lower, const float* exten
     const dpcull::pf::Box b = dpcull::pf::make_box(lower[i], lower[n + i], lower[2 * n + i],
                                                    extent[i], extent[n + i], extent[2 * n + i],
                                                    m0, m1, m2, m3);
-    out[i] = (int8_t)dpcull::pf::classify(b, p, ok, dpcull::pf::is_affine(m0, m1, m2, m3));
+    out[i] = (int8_t)dpcull::pf::classify(b, p);
   }
 }
