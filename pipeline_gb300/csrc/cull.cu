@@ -56,11 +56,11 @@ struct WarpShared {
   CullScene sc;                                          // the scene of the warp's last item
   CullView cv[kMaxViewsPerPass];                         // the item's views (matrices + outputs)
   pf::Planes pl[kMaxViewsPerPass];                       // prefilter planes of the views
-  uint32_t words[kItemTiles][kMaxViewsPerPass][kTileWords];  // the item's visibility words
+  uint32_t words[kMaxViewsPerPass][kItemTiles][kTileWords];  // the item's visibility words
   uint16_t queue[kQueueCap];                             // tile << 10 | object << 3 | view
 };
 static_assert(kTileObjects == 32 * kObjPerThread, "a tile is one warp's objects");
-static_assert(kItemTiles * kMaxViewsPerPass * kTileWords == 4 * 32, "four words per lane");
+static_assert(kItemTiles * kTileWords <= 32, "one word of a view's item per lane");
 
 __device__ __forceinline__ uint32_t find_scene(const CullScene* scenes, uint32_t n, uint32_t item)
 {
@@ -88,42 +88,51 @@ __device__ __forceinline__ bool exact_visible(const CullScene& sc, uint32_t i, c
   return obb_visible(o, vp);
 }
 
-// Prefilter of the lane's 4 boxes in each view of the item: visible objects into nib[v]
-// (bit k), undecided pairs into amb (bit 8k + v).  Branch-free per pair.
-template <int VPP>
-__device__ __forceinline__ void classify_views(const WarpShared& ws, const pf::Box (&bx)[kObjPerThread],
-                                               int nv, uint32_t valid, uint32_t (&nib)[VPP],
-                                               uint32_t& amb)
+// The lane's 4 visibility bits of one view (bit k = object k) into the tile's words of
+// that view in the item (warp shuffles; the lanes 0, 8, 16, 24 store).
+__device__ __forceinline__ void store_nibble(WarpShared& ws, int v, uint32_t t, uint32_t nib, int lane)
 {
+  uint32_t w = nib << ((lane & 7) * 4);
+  w |= __shfl_xor_sync(0xffffffffu, w, 1);
+  w |= __shfl_xor_sync(0xffffffffu, w, 2);
+  w |= __shfl_xor_sync(0xffffffffu, w, 4);
+  if ((lane & 7) == 0) ws.words[v][t][lane >> 3] = w;
+}
+
+// Prefilter of the lane's 4 boxes in each view of the item: visible objects into the
+// tile's words, undecided pairs into amb (bit 8k + v).  Branch-free per pair; the view
+// loop is not unrolled (nv is uniform over the warp).
+__device__ __forceinline__ void classify_views(WarpShared& ws, const pf::Box (&bx)[kObjPerThread],
+                                               int nv, uint32_t t, uint32_t valid, uint32_t& amb,
+                                               int lane)
+{
+#pragma unroll 1
+  for (int v = 0; v < nv; ++v) {
+    const pf::Planes& P = ws.pl[v];
+    const pf::F4 n01 = P.n01, n2g = P.n2g;
+    float mi[kObjPerThread], mo[kObjPerThread];
 #pragma unroll
-  for (int v = 0; v < VPP; ++v) {
-    if (v < nv) {
-      const pf::Planes& P = ws.pl[v];
-      const pf::F4 n01 = P.n01, n2g = P.n2g;
-      float mi[kObjPerThread], mo[kObjPerThread];
+    for (int k = 0; k < kObjPerThread; ++k) mi[k] = mo[k] = __int_as_float(0x7f800000);
 #pragma unroll
-      for (int k = 0; k < kObjPerThread; ++k) mi[k] = mo[k] = __int_as_float(0x7f800000);
+    for (int ax = 0; ax < 3; ++ax) {
+      const pf::F4 ql = P.q[ax][0], qh = P.q[ax][1];
+      const float nl = ax == 0 ? n01.x : ax == 1 ? n01.z : n2g.x;
+      const float nh = ax == 0 ? n01.y : ax == 1 ? n01.w : n2g.y;
 #pragma unroll
-      for (int ax = 0; ax < 3; ++ax) {
-        const pf::F4 ql = P.q[ax][0], qh = P.q[ax][1];
-        const float nl = ax == 0 ? n01.x : ax == 1 ? n01.z : n2g.x;
-        const float nh = ax == 0 ? n01.y : ax == 1 ? n01.w : n2g.y;
-#pragma unroll
-        for (int k = 0; k < kObjPerThread; ++k) pf::axis(bx[k], ql, qh, nl, nh, mi[k], mo[k]);
-      }
-      uint32_t in = 0, und = 0;
-#pragma unroll
-      for (int k = 0; k < kObjPerThread; ++k) {
-        const float d = bx[k].d0 + n2g.z;
-        const bool vis = mi[k] > d, out = mo[k] <= -d;
-        in |= (uint32_t)vis << k;
-        und |= (uint32_t)(!vis && !out) << k;
-      }
-      nib[v] = in & valid;
-      // bit k of und -> bit 8k (the multiply places each bit k at 8k; the mask drops the
-      // cross terms), then view v's column
-      amb |= (((und & valid) * 0x204081u) & 0x01010101u) << v;
+      for (int k = 0; k < kObjPerThread; ++k) pf::axis(bx[k], ql, qh, nl, nh, mi[k], mo[k]);
     }
+    uint32_t in = 0, und = 0;
+#pragma unroll
+    for (int k = 0; k < kObjPerThread; ++k) {
+      const float d = bx[k].d0 + n2g.z;
+      const bool vis = mi[k] > d, out = mo[k] <= -d;
+      in |= (uint32_t)vis << k;
+      und |= (uint32_t)(!vis && !out) << k;
+    }
+    // bit k of und -> bit 8k (the multiply places each bit k at 8k; the mask drops the
+    // cross terms), then view v's column
+    amb |= (((und & valid) * 0x204081u) & 0x01010101u) << v;
+    store_nibble(ws, v, t, in & valid, lane);
   }
 }
 
@@ -148,7 +157,7 @@ __device__ __forceinline__ void drain_queue(WarpShared& ws, const CullScene& sc,
     const uint32_t e = ws.queue[q];
     const uint32_t t = e >> 10, o = (e >> 3) & 127u, v = e & 7u;
     if (exact_visible(sc, (tile_first + t) * kTileObjects + o, ws.cv[v].vp))
-      atomicOr(&ws.words[t][v][o >> 5], 1u << (o & 31));
+      atomicOr(&ws.words[v][t][o >> 5], 1u << (o & 31));
   }
   __syncwarp();
 }
@@ -172,11 +181,7 @@ __device__ __forceinline__ uint32_t classify_tile(const CullLaunch& a, WarpShare
   const uint4 xf = ld_stream4u(soa + 6 * cap + obj0);
   const float4* mats = reinterpret_cast<const float4*>(sc.mats);
 
-  uint32_t nib[VPP];
-#pragma unroll
-  for (int v = 0; v < VPP; ++v) nib[v] = 0;
   uint32_t amb = 0;
-
   if (PF) {
     // Prefilter boxes of the 4 objects first (the 16 matrix gathers overlap), then each
     // view's planes are read once for all 4 objects.
@@ -202,36 +207,31 @@ __device__ __forceinline__ uint32_t classify_tile(const CullLaunch& a, WarpShare
                            comp(ez, k), m0, m1, m2, m3);
       valid |= (uint32_t)use << k;
     }
-    classify_views<VPP>(ws, bx, nv, valid, nib, amb);
+    classify_views(ws, bx, nv, t, valid, amb, lane);
   } else {
+    // Exact test only: every pair in the reference's operation order (the box is rebuilt
+    // per view from the loaded rows; the matrix reloads hit L1).
+    uint32_t use = 0;
 #pragma unroll
     for (int k = 0; k < kObjPerThread; ++k) {
       if (obj0 + k < sc.n_objects) {
-        const uint32_t mi = compu(xf, k);
-        if (mi < sc.n_mats) {
-          const float4* M = mats + 4 * (size_t)mi;
-          const Obb o = make_obb(comp(lx, k), comp(ly, k), comp(lz, k), comp(ex, k), comp(ey, k),
-                                 comp(ez, k), __ldg(M + 0), __ldg(M + 1), __ldg(M + 2), __ldg(M + 3));
-#pragma unroll
-          for (int v = 0; v < VPP; ++v)
-            if (v < nv && obb_visible(o, ws.cv[v].vp)) nib[v] |= 1u << k;
-        } else if (atomicOr(&a.ctl->error, kErrBadTransform) == 0) {
-          a.ctl->error_info = obj0 + k;
-        }
+        if (compu(xf, k) < sc.n_mats) use |= 1u << k;
+        else if (atomicOr(&a.ctl->error, kErrBadTransform) == 0) a.ctl->error_info = obj0 + k;
       }
     }
-  }
-
-  // The decided-visible words of the tile (warp shuffles), into the item's words.
-  const int shift = (lane & 7) * 4;
+#pragma unroll 1
+    for (int v = 0; v < nv; ++v) {
+      uint32_t nib = 0;
 #pragma unroll
-  for (int v = 0; v < VPP; ++v) {
-    if (v < nv) {  // nv is uniform over the warp, so the shuffles stay warp-uniform
-      uint32_t w = nib[v] << shift;
-      w |= __shfl_xor_sync(0xffffffffu, w, 1);
-      w |= __shfl_xor_sync(0xffffffffu, w, 2);
-      w |= __shfl_xor_sync(0xffffffffu, w, 4);
-      if ((lane & 7) == 0) ws.words[t][v][lane >> 3] = w;
+      for (int k = 0; k < kObjPerThread; ++k) {
+        if (use & (1u << k)) {
+          const float4* M = mats + 4 * (size_t)compu(xf, k);
+          const Obb o = make_obb(comp(lx, k), comp(ly, k), comp(lz, k), comp(ex, k), comp(ey, k),
+                                 comp(ez, k), __ldg(M + 0), __ldg(M + 1), __ldg(M + 2), __ldg(M + 3));
+          if (obb_visible(o, ws.cv[v].vp)) nib |= 1u << k;
+        }
+      }
+      store_nibble(ws, v, t, nib, lane);
     }
   }
 
@@ -257,36 +257,30 @@ __device__ __forceinline__ uint32_t classify_tile(const CullLaunch& a, WarpShare
   return qn;
 }
 
-// The final words of one tile of the item: the new words (stored only where they
-// changed), the delta words (old XOR new, every word) and the visible counts.
-template <int VPP>
-__device__ __forceinline__ void finish_tile(const WarpShared& ws, uint32_t tile, uint32_t t, int nv, int lane)
+// The final words of the item, per view: the new words (stored only where they changed),
+// the delta words (old XOR new, every word) and the visible count.  Lane l handles word
+// l & 3 of tile l >> 2, so a view's words are one coalesced load and store.
+__device__ __forceinline__ void finish_item(const WarpShared& ws, uint32_t tile_first, uint32_t n_t,
+                                            int nv, int lane)
 {
-  const uint32_t word = tile * kTileWords + (uint32_t)(lane >> 3);
-  const bool writer = (lane & 7) == 0;  // lanes 0, 8, 16, 24 own the tile's 4 words
-  // All previous words are loaded before any word is stored, so the loads are in flight
-  // together (a later view's load could not move above an earlier view's store).
-  uint32_t prevw[VPP];
-#pragma unroll
-  for (int v = 0; v < VPP; ++v)
-    prevw[v] = (v < nv && writer && !(ws.cv[v].flags & kViewNoChanged)) ? ws.cv[v].bits[word] : 0u;
-#pragma unroll
-  for (int v = 0; v < VPP; ++v) {
-    if (v < nv) {
-      const uint32_t w = ws.words[t][v][lane >> 3];
-      if (writer) {
-        if (ws.cv[v].flags & kViewNoChanged) {
-          ws.cv[v].bits[word] = w;
-        } else {
-          const uint32_t d = w ^ prevw[v];
-          if (d) ws.cv[v].bits[word] = w;
-          ws.cv[v].delta[word] = d;
-        }
+  const bool mine = (uint32_t)lane < n_t * kTileWords;
+  const uint32_t word = tile_first * kTileWords + (uint32_t)lane;
+#pragma unroll 1
+  for (int v = 0; v < nv; ++v) {
+    const CullView& cv = ws.cv[v];
+    const uint32_t w = mine ? (&ws.words[v][0][0])[lane] : 0u;
+    if (mine) {
+      if (cv.flags & kViewNoChanged) {
+        cv.bits[word] = w;
+      } else {
+        const uint32_t d = w ^ cv.bits[word];
+        if (d) cv.bits[word] = w;
+        cv.delta[word] = d;
       }
-      if (ws.cv[v].n_visible) {
-        const uint32_t cnt = __reduce_add_sync(0xffffffffu, writer ? (uint32_t)__popc(w) : 0u);
-        if (lane == 0 && cnt) atomicAdd(ws.cv[v].n_visible, cnt);
-      }
+    }
+    if (cv.n_visible) {
+      const uint32_t cnt = __reduce_add_sync(0xffffffffu, (uint32_t)__popc(w));
+      if (lane == 0 && cnt) atomicAdd(cv.n_visible, cnt);
     }
   }
 }
@@ -335,7 +329,7 @@ __device__ __forceinline__ void warp_item(const CullLaunch& a, uint32_t item, Wa
     qn = classify_tile<VPP, PF>(a, ws, sc, tile_first + t, t, tile_first, nv, qn, lane);
   if (PF && qn) drain_queue(ws, sc, tile_first, qn, lane);
   else __syncwarp();
-  for (uint32_t t = 0; t < n_t; ++t) finish_tile<VPP>(ws, tile_first + t, t, nv, lane);
+  finish_item(ws, tile_first, n_t, nv, lane);
 }
 
 template <int VPP, bool PF>
