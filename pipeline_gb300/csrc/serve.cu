@@ -5,14 +5,15 @@
 //   1. retires finished batches (event query): per-request visible counts (and kept
 //      visibility words) come back in pinned memory, the scenes' in-flight counts drop;
 //   2. if a stream is free, builds the next batch from the pending requests in arrival
-//      order: a request joins when its scene is resident or can be made resident within
-//      the budget (evicting least recently used scenes with no work in flight) and the
-//      batch's object-views stay under the cap; requests that cannot be admitted yet
-//      stay pending and later ones go ahead;
-//   3. launches the batch on that stream: uploads of newly admitted scenes (their
-//      readiness is an event other streams wait on), descriptor upload, one persistent
-//      cull launch over all (scene, view) pairs (the kernel of cull.cu with visibility
-//      words only), and the copy back.
+//      order: a request whose scene is not on the device starts the scene's upload on
+//      the upload stream (evicting least recently used scenes with no work in flight)
+//      and stays pending until the upload's event has completed, so misses never delay
+//      the hits batched with them; a request joins when its scene is on the device and
+//      the batch's object-views stay under the cap; requests that cannot be admitted
+//      yet stay pending and later ones go ahead;
+//   3. launches the batch on that stream: descriptor upload, one persistent cull launch
+//      over all (scene, view) pairs (the kernel of cull.cu with visibility words only),
+//      and the copy back.
 // Memory: scene buffers and per-batch outputs come from the device's stream-ordered
 // pool (cudaMallocAsync / cudaFreeAsync), so eviction never synchronises the device.
 #include <cuda_runtime.h>
@@ -23,6 +24,7 @@
 #include <condition_variable>
 #include <cstring>
 #include <deque>
+#include <list>
 #include <map>
 #include <mutex>
 #include <set>
@@ -59,9 +61,11 @@ struct Scene {
   const float* packed = nullptr; // the same layout in pinned host memory (shared)
   uint64_t bytes = 0;
   bool resident = false;
+  bool uploading = false;        // upload issued, not yet seen complete: not evictable
   int pending = 0;               // batches in flight that use it
   uint64_t last_use = 0;
   cudaEvent_t ready = nullptr;   // recorded after the upload
+  std::list<uint32_t>::iterator lru;  // position in the server's LRU list while resident
 };
 
 struct Request {
@@ -104,8 +108,19 @@ struct dpcull_server_s {
   uint32_t n_streams = 0;
   Slot slots[kMaxStreams];
 
-  std::mutex scenes_mu;
+  std::mutex scenes_mu;      // residency state; the worker holds it across CUDA calls
   std::deque<Scene> scenes;  // references stay valid as scenes are added
+  std::list<uint32_t> lru;   // resident scenes, least recently used first
+  cudaStream_t up_stream = nullptr;  // scene uploads and evictions
+  // What a submit checks (registered, size), under a lock the worker never takes, so a
+  // submit never waits on the worker's uploads or evictions.
+  struct SceneInfo {
+    bool registered = false;
+    uint64_t bytes = 0;
+    size_t cap = 0;
+  };
+  std::mutex info_mu;
+  std::vector<SceneInfo> info;
   std::map<std::pair<const void*, size_t>, uint32_t> max_index;
   // Pinned copies in the device layout, one per distinct set of host arrays.
   std::map<std::tuple<const void*, const void*, const void*, const void*, size_t>, float*> packed;
@@ -119,7 +134,7 @@ struct dpcull_server_s {
   std::vector<dpcull_completion> done;
   std::unordered_map<uint64_t, std::vector<std::vector<uint32_t>>> results;
 
-  uint64_t resident_bytes = 0, inflight_bytes = 0, tick = 0;
+  uint64_t resident_bytes = 0, inflight_bytes = 0, uploading_bytes = 0, tick = 0;
   std::atomic<uint64_t> submitted{0}, completed{0};
   dpcull_server_stats stats{};
   std::atomic<bool> stop{false};
@@ -134,35 +149,55 @@ int vpp_for(uint32_t max_views)
   return max_views <= 1 ? 1 : max_views <= 2 ? 2 : max_views <= 4 ? 4 : 8;
 }
 
-void evict(dpcull_server s, Scene& sc, cudaStream_t st)
+void evict(dpcull_server s, Scene& sc)
 {
-  cudaFreeAsync(sc.dev, st);
+  // Every batch that read the scene has retired (pending == 0), so its memory is free to
+  // go back to the pool in upload-stream order.
+  cudaFreeAsync(sc.dev, s->up_stream);
   sc.dev = nullptr;
   sc.resident = false;
+  s->lru.erase(sc.lru);
   s->resident_bytes -= sc.bytes;
   s->stats.scene_evictions++;
 }
 
-// Makes room for `need` more bytes, evicting least recently used idle scenes.
-bool make_room(dpcull_server s, uint64_t need, cudaStream_t st)
+// Makes room for `need` more bytes, evicting least recently used idle scenes.  With
+// `take_uploaded`, a scene whose upload finished but whose requests are still queued may
+// go too (they upload it again): admitting a ready request then never waits on uploads
+// that wait on admissions.
+bool make_room(dpcull_server s, uint64_t need, bool take_uploaded)
 {
   while (s->resident_bytes + s->inflight_bytes + need > s->budget) {
     Scene* victim = nullptr;
-    for (auto& sc : s->scenes)
-      if (sc.resident && sc.pending == 0 && (!victim || sc.last_use < victim->last_use)) victim = &sc;
+    for (uint32_t id : s->lru) {
+      Scene& sc = s->scenes[id];
+      if (sc.pending != 0) continue;
+      if (!sc.uploading || (take_uploaded && cudaEventQuery(sc.ready) == cudaSuccess)) {
+        victim = &sc;
+        break;
+      }
+    }
     if (!victim) return false;
-    evict(s, *victim, st);
+    if (victim->uploading) {
+      victim->uploading = false;
+      s->uploading_bytes -= victim->bytes;
+    }
+    evict(s, *victim);
   }
   return true;
 }
 
-void upload(dpcull_server s, Scene& sc, cudaStream_t st)
+// Starts the upload of a scene on the upload stream (one copy from its pinned image).
+void upload(dpcull_server s, Scene& sc, uint32_t id)
 {
-  cudaMallocAsync((void**)&sc.dev, sc.bytes, st);
-  cudaMemcpyAsync(sc.dev, sc.packed, sc.bytes, cudaMemcpyHostToDevice, st);
+  cudaMallocAsync((void**)&sc.dev, sc.bytes, s->up_stream);
+  cudaMemcpyAsync(sc.dev, sc.packed, sc.bytes, cudaMemcpyHostToDevice, s->up_stream);
   if (!sc.ready) cudaEventCreateWithFlags(&sc.ready, cudaEventDisableTiming);
-  cudaEventRecord(sc.ready, st);
+  cudaEventRecord(sc.ready, s->up_stream);
   sc.resident = true;
+  sc.uploading = true;
+  s->uploading_bytes += sc.bytes;
+  sc.lru = s->lru.insert(s->lru.end(), id);
   s->resident_bytes += sc.bytes;
   s->stats.scene_uploads++;
   s->stats.upload_bytes += sc.bytes;
@@ -225,7 +260,6 @@ void copy_kept(Slot& slot)
 bool launch(dpcull_server s, Slot& slot)
 {
   std::vector<Request> take;
-  std::vector<uint32_t> new_scenes;
   uint64_t work = 0, out_bytes = 0;
   uint32_t max_views = 1;
   // Take the pending requests out under the lock, decide outside it (submitters never
@@ -241,6 +275,22 @@ bool launch(dpcull_server s, Slot& slot)
     bool full = false;
     for (auto& q : cand) {
       Scene& sc = s->scenes[q.scene];
+      // A scene that is not on the device yet starts its upload now and its requests wait
+      // in the queue; the batch goes ahead with the scenes that are ready, so a miss never
+      // holds up the hits of the same batch.
+      // At most half the budget is in uploads that no batch has taken yet (any one scene
+      // may upload alone).
+      if (!sc.resident) {
+        if ((s->uploading_bytes == 0 || s->uploading_bytes + sc.bytes <= s->budget / 2) &&
+            make_room(s, sc.bytes, false))
+          upload(s, sc, q.scene);
+        left.push_back(q);
+        continue;
+      }
+      if (sc.uploading && cudaEventQuery(sc.ready) != cudaSuccess) {
+        left.push_back(q);
+        continue;
+      }
       const uint64_t w = (uint64_t)sc.n * q.n_views;
       if (full || take.size() >= kMaxBatchRequests || (!take.empty() && work + w > s->max_batch)) {
         full = true;
@@ -248,17 +298,20 @@ bool launch(dpcull_server s, Slot& slot)
         continue;
       }
       const uint64_t ob = (uint64_t)q.n_views * (sc.cap / 8 + 4) + 256;  // >= its share of d_out
-      const uint64_t need = ob + (sc.resident ? 0 : sc.bytes);
-      if (!make_room(s, need, slot.stream)) {
+      sc.pending++;  // not a victim of its own admission
+      const bool room = make_room(s, ob, true);
+      sc.pending--;
+      if (!room) {
         left.push_back(q);  // cannot be admitted yet: later requests may go ahead
         continue;
       }
-      if (!sc.resident) {
-        upload(s, sc, slot.stream);
-        new_scenes.push_back(q.scene);
+      if (sc.uploading) {
+        sc.uploading = false;
+        s->uploading_bytes -= sc.bytes;
       }
       sc.pending++;
       sc.last_use = ++s->tick;
+      s->lru.splice(s->lru.end(), s->lru, sc.lru);  // most recently used
       s->inflight_bytes += ob;
       out_bytes += ob;
       work += w;
@@ -272,12 +325,7 @@ bool launch(dpcull_server s, Slot& slot)
   }
   if (take.empty()) return false;
 
-  // Scenes uploaded by other streams must be ready before this batch reads them.
-  for (auto& q : take) {
-    Scene& sc = s->scenes[q.scene];
-    if (sc.ready && std::find(new_scenes.begin(), new_scenes.end(), q.scene) == new_scenes.end())
-      cudaStreamWaitEvent(slot.stream, sc.ready, 0);
-  }
+  // Every scene of the batch was seen uploaded (its event complete) before admission.
   size_t n_views = 0;
   for (auto& q : take) n_views += q.n_views;
   cudaMallocAsync((void**)&slot.d_out, out_bytes, slot.stream);
@@ -398,7 +446,8 @@ void worker_main(dpcull_server s)
       bool busy = false;
       for (uint32_t i = 0; i < s->n_streams; ++i) busy |= s->slots[i].busy;
       std::unique_lock<std::mutex> lk(s->pending_mu);
-      if (busy) s->pending_cv.wait_for(lk, std::chrono::microseconds(5));
+      // Requests waiting for uploads are polled like batches in flight.
+      if (busy || !s->pending.empty()) s->pending_cv.wait_for(lk, std::chrono::microseconds(5));
       else s->pending_cv.wait_for(lk, std::chrono::microseconds(200), [&] { return !s->pending.empty() || s->stop.load(); });
     }
   }
@@ -427,6 +476,12 @@ int dpcull_server_create(dpcull_ctx ctx, uint64_t budget_bytes, uint32_t n_strea
   if (cudaDeviceGetDefaultMemPool(&pool, s->device) == cudaSuccess) {
     uint64_t keep = ~0ull;  // keep freed blocks for reuse instead of returning them
     cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &keep);
+  }
+  if (cudaStreamCreateWithFlags(&s->up_stream, cudaStreamNonBlocking) != cudaSuccess) {
+    cudaGetLastError();
+    s->n_streams = 0;
+    dpcull_server_destroy(s);
+    return record_error(DPCULL_ERR_CUDA, "dpcull_server_create: stream set-up failed");
   }
   for (uint32_t i = 0; i < n_streams; ++i) {
     Slot& sl = s->slots[i];
@@ -460,10 +515,12 @@ int dpcull_server_destroy(dpcull_server s)
     Slot& sl = s->slots[i];
     if (sl.stream) cudaStreamSynchronize(sl.stream);
   }
+  if (s->up_stream) cudaStreamSynchronize(s->up_stream);
   for (auto& sc : s->scenes) {
-    if (sc.dev) cudaFreeAsync(sc.dev, s->slots[0].stream);
+    if (sc.dev) cudaFree(sc.dev);
     if (sc.ready) cudaEventDestroy(sc.ready);
   }
+  if (s->up_stream) cudaStreamDestroy(s->up_stream);
   for (uint32_t i = 0; i < s->n_streams; ++i) {
     Slot& sl = s->slots[i];
     if (sl.stream) cudaStreamSynchronize(sl.stream);
@@ -535,6 +592,11 @@ int dpcull_server_add_scene(dpcull_server s, uint32_t scene, size_t n, const flo
     pk = s->packed.emplace(pkey, p).first;
   }
   sc.packed = pk->second;
+  {
+    std::lock_guard<std::mutex> li(s->info_mu);
+    if (scene >= s->info.size()) s->info.resize(scene + 1);
+    s->info[scene] = dpcull_server_s::SceneInfo{true, sc.bytes, sc.cap};
+  }
   return DPCULL_OK;
 }
 
@@ -544,10 +606,10 @@ int dpcull_server_submit(dpcull_server s, uint32_t scene, uint32_t n_views, cons
   if (!s || !vps || !n_views || n_views > DPCULL_SERVER_MAX_VIEWS)
     return record_error(DPCULL_ERR_INVALID_ARGUMENT, "dpcull_server_submit: 1..8 views");
   {
-    std::lock_guard<std::mutex> lk(s->scenes_mu);
-    if (scene >= s->scenes.size() || !s->scenes[scene].registered)
+    std::lock_guard<std::mutex> lk(s->info_mu);
+    if (scene >= s->info.size() || !s->info[scene].registered)
       return record_error(DPCULL_ERR_INVALID_ARGUMENT, "dpcull_server_submit: unknown scene");
-    const Scene& sc = s->scenes[scene];
+    const auto& sc = s->info[scene];
     if (sc.bytes + n_views * (sc.cap / 8 + 4) > s->budget)
       return record_error(DPCULL_ERR_CAPACITY, "dpcull_server_submit: the scene does not fit the budget");
   }
