@@ -167,6 +167,11 @@ int dpcull_plan_set_views(dpcull_ctx ctx, dpcull_plan p, const float* vps);
 /* (async) Replays the plan's graph. */
 int dpcull_plan_launch(dpcull_ctx ctx, dpcull_plan p);
 int dpcull_plan_tuning(dpcull_ctx ctx, dpcull_plan p, dpcull_tuning* out);
+/* Duration in ms of the cull kernel alone in one of the plan's two most recent launches
+ * (back = 0: the last one, 1: the one before), from CUDA events that the plan's graph
+ * records right before and after the kernel; waits until that kernel has finished.  No
+ * counterpart in the reference (measurement for the kernel's roofline). */
+int dpcull_plan_kernel_ms(dpcull_ctx ctx, dpcull_plan p, uint32_t back, float* ms);
 int dpcull_plan_destroy(dpcull_ctx ctx, dpcull_plan p);
 /* Autotunes views_per_pass / tiles_per_ticket / ctas_per_sm for the job list by timing
  * candidate launches (results of the jobs are overwritten). */

@@ -120,6 +120,7 @@ struct Plan {
   CullView* h_views[2] = {nullptr, nullptr};   // pinned, double buffered
   cudaGraphExec_t exec[2] = {nullptr, nullptr};
   cudaEvent_t done[2] = {nullptr, nullptr};
+  cudaEvent_t kt[2][2] = {{nullptr, nullptr}, {nullptr, nullptr}};  // cull kernel begin / end
   bool pending[2] = {false, false};
   bool fresh[2] = {false, false};      // slot holds matrices from set_views
   std::vector<uint32_t> all_groups;    // every job's group (empty ones included)
@@ -471,9 +472,12 @@ int persistent_grid(dpcull_ctx c, uint32_t vpp, uint32_t ctas_per_sm, uint32_t n
 }
 
 // The cull over all scenes and views, then the changed-list assembly of every view.
+// k0 / k1 (optional, timing events) are recorded right before and after the cull kernel;
+// inside a stream capture they become event-record nodes visible outside the graph.
 int launch_batch(dpcull_ctx c, const CullScene* d_scenes, const CullView* d_views,
                  uint32_t n_scenes, uint32_t n_views, uint32_t max_words, uint32_t n_items,
-                 const dpcull_tuning& t, cudaStream_t s)
+                 const dpcull_tuning& t, cudaStream_t s, cudaEvent_t k0 = nullptr,
+                 cudaEvent_t k1 = nullptr)
 {
   if (n_views > 65535) return fail(DPCULL_ERR_INVALID_ARGUMENT, "at most 65535 views per launch");
   CullLaunch a{};
@@ -485,7 +489,9 @@ int launch_batch(dpcull_ctx c, const CullScene* d_scenes, const CullView* d_view
   a.exact_only = c->exact_only ? 1u : 0u;
   a.ctl = c->ctl;
   const int grid = persistent_grid(c, t.views_per_pass, t.ctas_per_sm, n_items, a.items_per_ticket);
+  if (k0) CU(cudaEventRecordWithFlags(k0, s, cudaEventRecordExternal));
   if (launch_cull(a, grid, (int)t.views_per_pass, s)) return cuda_fail(cudaGetLastError(), "cull launch");
+  if (k1) CU(cudaEventRecordWithFlags(k1, s, cudaEventRecordExternal));
   CullView none{};
   if (launch_changed_lists(d_views, none, n_views, max_words, s))
     return cuda_fail(cudaGetLastError(), "changed-list launch");
@@ -1087,7 +1093,7 @@ static int plan_capture(dpcull_ctx c, Plan& p, int slot)
   if (e == cudaSuccess) {
     const uint64_t before = c->launches;
     rc = launch_batch(c, p.d_scenes, p.d_views, (uint32_t)p.scenes.size(), (uint32_t)p.views.size(),
-                      max_words_of(p.scenes), p.n_items, p.tuning, cs);
+                      max_words_of(p.scenes), p.n_items, p.tuning, cs, p.kt[slot][0], p.kt[slot][1]);
     c->launches = before;  // counted when the graph is replayed
   }
   cudaError_t e2 = cudaStreamEndCapture(cs, &graph);
@@ -1231,6 +1237,8 @@ int dpcull_plan_create(dpcull_ctx c, const dpcull_job* jobs, size_t n_jobs,
     CU(cudaMallocHost((void**)&p.h_views[s], p.views.size() * sizeof(CullView)));
     memcpy(p.h_views[s], p.views.data(), p.views.size() * sizeof(CullView));
     CU(cudaEventCreateWithFlags(&p.done[s], cudaEventDisableTiming));
+    CU(cudaEventCreate(&p.kt[s][0]));
+    CU(cudaEventCreate(&p.kt[s][1]));
     rc = plan_capture(c, p, s);
     if (rc) return rc;
   }
@@ -1290,6 +1298,17 @@ int dpcull_plan_launch(dpcull_ctx c, dpcull_plan ph)
   return DPCULL_OK;
 }
 
+int dpcull_plan_kernel_ms(dpcull_ctx c, dpcull_plan ph, uint32_t back, float* ms)
+{
+  Plan* p = get_plan(c, ph);
+  if (!p || !ms || back > 1) return fail(DPCULL_ERR_INVALID_ARGUMENT, "bad plan %u or argument", ph);
+  const int s = back ? p->next : p->next ^ 1;  // the last launch used next ^ 1
+  if (!p->pending[s]) return fail(DPCULL_ERR_STATE, "no such launch of plan %u", ph);
+  CU(cudaEventSynchronize(p->kt[s][1]));
+  CU(cudaEventElapsedTime(ms, p->kt[s][0], p->kt[s][1]));
+  return DPCULL_OK;
+}
+
 int dpcull_plan_tuning(dpcull_ctx c, dpcull_plan ph, dpcull_tuning* out)
 {
   Plan* p = get_plan(c, ph);
@@ -1306,6 +1325,8 @@ int dpcull_plan_destroy(dpcull_ctx c, dpcull_plan ph)
   for (int s = 0; s < 2; ++s) {
     if (p->exec[s]) cudaGraphExecDestroy(p->exec[s]);
     if (p->done[s]) cudaEventDestroy(p->done[s]);
+    if (p->kt[s][0]) cudaEventDestroy(p->kt[s][0]);
+    if (p->kt[s][1]) cudaEventDestroy(p->kt[s][1]);
     if (p->h_views[s]) cudaFreeHost(p->h_views[s]);
   }
   dfree(c, p->d_scenes, p->scenes.size() * sizeof(CullScene));

@@ -82,6 +82,7 @@ _SIGS = {
     "dpcull_plan_set_views": (_I, [_P, _U32, _FP]),
     "dpcull_plan_launch": (_I, [_P, _U32]),
     "dpcull_plan_tuning": (_I, [_P, _U32, C.POINTER(Tuning)]),
+    "dpcull_plan_kernel_ms": (_I, [_P, _U32, _U32, C.POINTER(C.c_float)]),
     "dpcull_plan_destroy": (_I, [_P, _U32]),
     "dpcull_autotune": (_I, [_P, C.POINTER(Job), _SZ, C.POINTER(Tuning)]),
     "dpcull_tree_create": (_I, [_P, _SZ, _UP]),
@@ -353,6 +354,12 @@ class Context:
 
     def plan_launch(self, p: int) -> None:
         _check(self.lib.dpcull_plan_launch(self.h, p))
+
+    def plan_kernel_ms(self, p: int, back: int = 0) -> float:
+        """Cull-kernel duration (ms) of the plan's last (back=0) or previous (back=1) launch."""
+        ms = C.c_float()
+        _check(self.lib.dpcull_plan_kernel_ms(self.h, p, back, C.byref(ms)))
+        return ms.value
 
     def plan_tuning(self, p: int) -> dict:
         t = Tuning()

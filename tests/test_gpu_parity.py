@@ -203,6 +203,9 @@ def test_plan_graph_frames(ctx):
     ctx.plan_launch(p)
     for v in range(8):
         assert len(ctx.result_changed(rs[v])) == 0
+    # the cull kernel's own duration, from events inside the graph, for both kept launches
+    k0, k1 = ctx.plan_kernel_ms(p, 0), ctx.plan_kernel_ms(p, 1)
+    assert 0.0 < k0 < 1000.0 and 0.0 < k1 < 1000.0
     ctx.plan_destroy(p)
     ctx.group_destroy(g)
 
