@@ -259,28 +259,36 @@ __device__ __forceinline__ uint32_t classify_tile(const CullLaunch& a, WarpShare
 
 // The final words of the item, per view: the new words (stored only where they changed),
 // the delta words (old XOR new, every word) and the visible count.  Lane l handles word
-// l & 3 of tile l >> 2, so a view's words are one coalesced load and store.
+// l & 3 of tile l >> 2, so a view's words are one coalesced load and store.  Every view's
+// previous words are loaded before any store, so the loads are in flight together.
+template <int VPP>
 __device__ __forceinline__ void finish_item(const WarpShared& ws, uint32_t tile_first, uint32_t n_t,
                                             int nv, int lane)
 {
   const bool mine = (uint32_t)lane < n_t * kTileWords;
   const uint32_t word = tile_first * kTileWords + (uint32_t)lane;
-#pragma unroll 1
-  for (int v = 0; v < nv; ++v) {
-    const CullView& cv = ws.cv[v];
-    const uint32_t w = mine ? (&ws.words[v][0][0])[lane] : 0u;
-    if (mine) {
-      if (cv.flags & kViewNoChanged) {
-        cv.bits[word] = w;
-      } else {
-        const uint32_t d = w ^ cv.bits[word];
-        if (d) cv.bits[word] = w;
-        cv.delta[word] = d;
+  uint32_t prev[VPP];
+#pragma unroll
+  for (int v = 0; v < VPP; ++v)
+    prev[v] = (v < nv && mine && !(ws.cv[v].flags & kViewNoChanged)) ? ws.cv[v].bits[word] : 0u;
+#pragma unroll
+  for (int v = 0; v < VPP; ++v) {
+    if (v < nv) {
+      const CullView& cv = ws.cv[v];
+      const uint32_t w = mine ? (&ws.words[v][0][0])[lane] : 0u;
+      if (mine) {
+        if (cv.flags & kViewNoChanged) {
+          cv.bits[word] = w;
+        } else {
+          const uint32_t d = w ^ prev[v];
+          if (d) cv.bits[word] = w;
+          cv.delta[word] = d;
+        }
       }
-    }
-    if (cv.n_visible) {
-      const uint32_t cnt = __reduce_add_sync(0xffffffffu, (uint32_t)__popc(w));
-      if (lane == 0 && cnt) atomicAdd(cv.n_visible, cnt);
+      if (cv.n_visible) {
+        const uint32_t cnt = __reduce_add_sync(0xffffffffu, (uint32_t)__popc(w));
+        if (lane == 0 && cnt) atomicAdd(cv.n_visible, cnt);
+      }
     }
   }
 }
@@ -329,7 +337,7 @@ __device__ __forceinline__ void warp_item(const CullLaunch& a, uint32_t item, Wa
     qn = classify_tile<VPP, PF>(a, ws, sc, tile_first + t, t, tile_first, nv, qn, lane);
   if (PF && qn) drain_queue(ws, sc, tile_first, qn, lane);
   else __syncwarp();
-  finish_item(ws, tile_first, n_t, nv, lane);
+  finish_item<VPP>(ws, tile_first, n_t, nv, lane);
 }
 
 template <int VPP, bool PF>
