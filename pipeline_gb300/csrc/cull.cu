@@ -111,13 +111,16 @@ __device__ __forceinline__ void classify_views(WarpShared& ws, const pf::Box (&b
     const pf::Planes& P = ws.pl[v];
     const pf::F4 n01 = P.n01, n2g = P.n2g;
     float mi[kObjPerThread], mo[kObjPerThread];
+    {
+      const pf::F4 ql = P.q[0][0], qh = P.q[0][1];
 #pragma unroll
-    for (int k = 0; k < kObjPerThread; ++k) mi[k] = mo[k] = __int_as_float(0x7f800000);
+      for (int k = 0; k < kObjPerThread; ++k) pf::axis<true>(bx[k], ql, qh, n01.x, n01.y, mi[k], mo[k]);
+    }
 #pragma unroll
-    for (int ax = 0; ax < 3; ++ax) {
+    for (int ax = 1; ax < 3; ++ax) {
       const pf::F4 ql = P.q[ax][0], qh = P.q[ax][1];
-      const float nl = ax == 0 ? n01.x : ax == 1 ? n01.z : n2g.x;
-      const float nh = ax == 0 ? n01.y : ax == 1 ? n01.w : n2g.y;
+      const float nl = ax == 1 ? n01.z : n2g.x;
+      const float nh = ax == 1 ? n01.w : n2g.y;
 #pragma unroll
       for (int k = 0; k < kObjPerThread; ++k) pf::axis(bx[k], ql, qh, nl, nh, mi[k], mo[k]);
     }

@@ -157,10 +157,25 @@ struct Box {
   float r, d0;
 };
 
+// Square root for the upper bounds below: on the GPU the hardware approximation
+// (sqrt.approx.f32; tests/test_gpu_prefilter_sqrt.py checks every input in [2^-120, 2^127]
+// against the correctly rounded root: relative error below 2^-21, so the 2^-18 inflation
+// that follows every use keeps the bound), on the host the correctly rounded one.
+DPCULL_HD float sqrt_bound(float x)
+{
+#if defined(__CUDA_ARCH__)
+  float r;
+  asm("sqrt.approx.f32 %0, %1;" : "=f"(r) : "f"(x));
+  return r;
+#else
+  return std::sqrt(x);
+#endif
+}
+
 // Upper bound of ||(r.x, r.y, r.z)||: the 2^-120 addend keeps every partial sum normal.
 DPCULL_HD float row_norm(const F4& m)
 {
-  return std::sqrt(std::fma(m.x, m.x, std::fma(m.y, m.y, std::fma(m.z, m.z, 0x1p-120f)))) * kInflate;
+  return sqrt_bound(std::fma(m.x, m.x, std::fma(m.y, m.y, std::fma(m.z, m.z, 0x1p-120f)))) * kInflate;
 }
 
 // True when the matrix maps w = 1 to w = 1 and directions to w = 0 (no projective part).
@@ -172,7 +187,7 @@ DPCULL_HD bool is_affine(const F4& m0, const F4& m1, const F4& m2, const F4& m3)
 DPCULL_HD Box make_box(float lx, float ly, float lz, float ex, float ey, float ez, const F4& m0,
                        const F4& m1, const F4& m2, const F4& m3)
 {
-  const float cx0 = lx + 0.5f * ex, cy0 = ly + 0.5f * ey, cz0 = lz + 0.5f * ez;
+  const float cx0 = std::fma(0.5f, ex, lx), cy0 = std::fma(0.5f, ey, ly), cz0 = std::fma(0.5f, ez, lz);
   Box b;
   b.cx = std::fma(cz0, m2.x, std::fma(cy0, m1.x, std::fma(cx0, m0.x, m3.x)));
   b.cy = std::fma(cz0, m2.y, std::fma(cy0, m1.y, std::fma(cx0, m0.y, m3.y)));
@@ -192,6 +207,7 @@ DPCULL_HD Box make_box(float lx, float ly, float lz, float ex, float ey, float e
 //   candidate min(t_lo, max(t_hi, -s_lo)).
 // c.w == 1: Q_w is the addend of L; E = R q, and t = fl(L + R q), s = fl(L - R q) are one
 // rounding each.
+template <bool kFirst = false>
 DPCULL_HD void axis(const Box& b, const F4& ql, const F4& qh, float nl, float nh, float& mi,
                     float& mo)
 {
@@ -199,8 +215,13 @@ DPCULL_HD void axis(const Box& b, const F4& ql, const F4& qh, float nl, float nh
   const float Lh = std::fma(b.cz, qh.z, std::fma(b.cy, qh.y, std::fma(b.cx, qh.x, qh.w)));
   const float tl = std::fma(b.r, nl, Ll), sl = std::fma(-b.r, nl, Ll);
   const float th = std::fma(b.r, nh, Lh);
-  mo = std::fmin(mo, std::fmin(tl, std::fmax(th, -sl)));
-  mi = std::fmin(mi, std::fmin(Ll, Lh));
+  if (kFirst) {  // the first axis starts the minima
+    mo = std::fmin(tl, std::fmax(th, -sl));
+    mi = std::fmin(Ll, Lh);
+  } else {
+    mo = std::fmin(mo, std::fmin(tl, std::fmax(th, -sl)));
+    mi = std::fmin(mi, std::fmin(Ll, Lh));
+  }
 }
 
 enum : int { kInvisible = 0, kVisible = 1, kUndecided = 2 };
@@ -209,10 +230,10 @@ enum : int { kInvisible = 0, kVisible = 1, kUndecided = 2 };
 // the view's planes shared by several boxes).
 DPCULL_HD int classify(const Box& b, const Planes& p)
 {
-  const float inf = INFINITY;
   const float d = b.d0 + p.n2g.z;
-  float mi = inf, mo = inf;
-  for (int a = 0; a < 3; ++a) axis(b, p.q[a][0], p.q[a][1], p.qlo(a), p.qhi(a), mi, mo);
+  float mi, mo;
+  axis<true>(b, p.q[0][0], p.q[0][1], p.qlo(0), p.qhi(0), mi, mo);
+  for (int a = 1; a < 3; ++a) axis(b, p.q[a][0], p.q[a][1], p.qlo(a), p.qhi(a), mi, mo);
   if (mi > d) return kVisible;
   if (mo <= -d) return kInvisible;
   return kUndecided;
