@@ -318,15 +318,13 @@ def run_e2e(ctx, wl, frames, args, dist) -> dict:
         vps_pinned[:] = frames[i % len(frames)]
         ctx.plan_set_views(wl.plan, vps_pinned)
         ctx.plan_launch(wl.plan)
-        for v in range(wl.v):
-            ctx.result_bits(wl.rs[v], bits[v])
-            ch = ctx.result_changed(wl.rs[v], changed[v])
-            d2h += words * 4 + 4 + 4 * len(ch)
+        n_ch = ctx.plan_read(wl.plan, bits, changed)
+        d2h += wl.v * (words * 4 + 4) + 4 * int(n_ch.sum())
     dt = dist.max(time.perf_counter() - t0)
     return {"value": wl.object_views() * dist.world * steps / dt, "unit": "object-views/s",
             "ms_per_step": dt * 1e3 / steps, "h2d_bytes_per_step": wl.v * 64,
             "d2h_bytes_per_step": int(d2h / steps), "steps": steps,
-            "path": "plan_set_views + plan_launch + result_bits + result_changed (C ABI)"}
+            "path": "plan_set_views + plan_launch + plan_read (every view's words and changed list; C ABI)"}
 
 
 def traffic_from_profile(wl) -> int | None:

@@ -172,6 +172,15 @@ int dpcull_plan_tuning(dpcull_ctx ctx, dpcull_plan p, dpcull_tuning* out);
  * records right before and after the kernel; waits until that kernel has finished.  No
  * counterpart in the reference (measurement for the kernel's roofline). */
 int dpcull_plan_kernel_ms(dpcull_ctx ctx, dpcull_plan p, uint32_t back, float* ms);
+/* Reads the results of the plan's last launch to the host in two waits: result i is the
+ * i-th result of the plan's jobs in job and view order.  bits[i] (ceil(objects/32) words)
+ * and changed[i] (changed_cap[i] entries) may be NULL to skip; n_changed[i] receives the
+ * length of the changed list.  Pinned host buffers copy fastest.  Equivalent to
+ * dpcull_result_bits + dpcull_result_changed on every result (ResultBitSet's
+ * getChanged, dp/culling/src/ResultBitSet.cpp:61-108), with one wait per kind of data
+ * instead of one or two per result.  DPCULL_ERR_CAPACITY when a list does not fit. */
+int dpcull_plan_read(dpcull_ctx ctx, dpcull_plan p, uint32_t* const* bits, uint32_t* const* changed,
+                     const size_t* changed_cap, size_t* n_changed);
 int dpcull_plan_destroy(dpcull_ctx ctx, dpcull_plan p);
 /* Autotunes views_per_pass / tiles_per_ticket / ctas_per_sm for the job list by timing
  * candidate launches (results of the jobs are overwritten). */

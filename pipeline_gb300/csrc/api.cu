@@ -124,6 +124,8 @@ struct Plan {
   bool pending[2] = {false, false};
   bool fresh[2] = {false, false};      // slot holds matrices from set_views
   std::vector<uint32_t> all_groups;    // every job's group (empty ones included)
+  std::vector<uint32_t> all_results;   // every job's results, in job and view order
+  uint32_t* h_counts = nullptr;        // pinned: changed counts read by dpcull_plan_read
   std::vector<uint64_t> all_incarnations;
   int next = 0;
   dpcull_tuning tuning{};
@@ -1228,7 +1230,9 @@ int dpcull_plan_create(dpcull_ctx c, const dpcull_job* jobs, size_t n_jobs,
   for (size_t j = 0; j < n_jobs; ++j) {
     p.all_groups.push_back(jobs[j].group);
     p.all_incarnations.push_back(c->groups[jobs[j].group].incarnation);
+    for (uint32_t v = 0; v < jobs[j].n_views; ++v) p.all_results.push_back(jobs[j].results[v]);
   }
+  CU(cudaMallocHost((void**)&p.h_counts, (p.all_results.size() + 2) * sizeof(uint32_t)));
   rc = dalloc(c, (void**)&p.d_scenes, p.scenes.size() * sizeof(CullScene));
   if (!rc) rc = dalloc(c, (void**)&p.d_views, p.views.size() * sizeof(CullView));
   if (rc) return rc;
@@ -1309,6 +1313,43 @@ int dpcull_plan_kernel_ms(dpcull_ctx c, dpcull_plan ph, uint32_t back, float* ms
   return DPCULL_OK;
 }
 
+int dpcull_plan_read(dpcull_ctx c, dpcull_plan ph, uint32_t* const* bits, uint32_t* const* changed,
+                     const size_t* changed_cap, size_t* n_changed)
+{
+  Plan* p = get_plan(c, ph);
+  if (!p) return fail(DPCULL_ERR_INVALID_ARGUMENT, "bad plan %u", ph);
+  const size_t nr = p->all_results.size();
+  std::vector<Result*> rs(nr);
+  for (size_t i = 0; i < nr; ++i) {
+    rs[i] = get_result(c, p->all_results[i]);
+    if (!rs[i]) return fail(DPCULL_ERR_STATE, "plan %u: result %u was destroyed", ph, p->all_results[i]);
+  }
+  // 1. every changed count and the device error word, one wait
+  for (size_t i = 0; i < nr; ++i)
+    CU(cudaMemcpyAsync(p->h_counts + i, rs[i]->n_changed, 4, cudaMemcpyDeviceToHost, c->stream));
+  CU(cudaMemcpyAsync(p->h_counts + nr, &c->ctl->error, 2 * sizeof(unsigned int), cudaMemcpyDeviceToHost,
+                     c->stream));
+  CU(cudaStreamSynchronize(c->stream));
+  if (p->h_counts[nr]) return check_device_errors(c);
+  // 2. every requested array, one wait
+  for (size_t i = 0; i < nr; ++i) {
+    const uint32_t cnt = p->h_counts[i];
+    if (n_changed) n_changed[i] = cnt;
+    if (bits && bits[i] && rs[i]->size_bits)
+      CU(cudaMemcpyAsync(bits[i], rs[i]->bits, (rs[i]->size_bits + 31) / 32 * 4, cudaMemcpyDeviceToHost,
+                         c->stream));
+    if (changed && changed[i] && cnt) {
+      if (!changed_cap || cnt > changed_cap[i]) {
+        CU(cudaStreamSynchronize(c->stream));
+        return fail(DPCULL_ERR_CAPACITY, "plan %u: result %zu has %u changed objects", ph, i, cnt);
+      }
+      CU(cudaMemcpyAsync(changed[i], rs[i]->changed, (size_t)cnt * 4, cudaMemcpyDeviceToHost, c->stream));
+    }
+  }
+  CU(cudaStreamSynchronize(c->stream));
+  return DPCULL_OK;
+}
+
 int dpcull_plan_tuning(dpcull_ctx c, dpcull_plan ph, dpcull_tuning* out)
 {
   Plan* p = get_plan(c, ph);
@@ -1329,6 +1370,7 @@ int dpcull_plan_destroy(dpcull_ctx c, dpcull_plan ph)
     if (p->kt[s][1]) cudaEventDestroy(p->kt[s][1]);
     if (p->h_views[s]) cudaFreeHost(p->h_views[s]);
   }
+  if (p->h_counts) cudaFreeHost(p->h_counts);
   dfree(c, p->d_scenes, p->scenes.size() * sizeof(CullScene));
   dfree(c, p->d_views, p->views.size() * sizeof(CullView));
   *p = Plan();

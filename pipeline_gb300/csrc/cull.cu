@@ -170,18 +170,22 @@ __device__ __forceinline__ void drain_queue(WarpShared& ws, const CullScene& sc,
 template <int VPP, bool PF>
 __device__ __forceinline__ uint32_t classify_tile(const CullLaunch& a, WarpShared& ws, const CullScene& sc,
                                                   uint32_t tile, uint32_t t, uint32_t tile_first,
-                                                  int nv, uint32_t qn, int lane)
+                                                  uint32_t n_t, int nv, uint32_t qn, int lane,
+                                                  const uint4 xf_cur, uint4& xf_next)
 {
   const uint32_t obj0 = tile * kTileObjects + (uint32_t)lane * kObjPerThread;
   const float* soa = sc.soa;
   const size_t cap = sc.cap;
+  // The transform indices of this tile were loaded one tile ahead, so the matrix gathers
+  // below go out together with the other rows; the next tile's indices go out now.
+  const uint4 xf = xf_cur;
+  if (t + 1 < n_t) xf_next = ld_stream4u(soa + 6 * cap + obj0 + kTileObjects);
   const float4 lx = ld_stream4(soa + 0 * cap + obj0);
   const float4 ly = ld_stream4(soa + 1 * cap + obj0);
   const float4 lz = ld_stream4(soa + 2 * cap + obj0);
   const float4 ex = ld_stream4(soa + 3 * cap + obj0);
   const float4 ey = ld_stream4(soa + 4 * cap + obj0);
   const float4 ez = ld_stream4(soa + 5 * cap + obj0);
-  const uint4 xf = ld_stream4u(soa + 6 * cap + obj0);
   const float4* mats = reinterpret_cast<const float4*>(sc.mats);
 
   uint32_t amb = 0;
@@ -319,6 +323,8 @@ __device__ __forceinline__ void warp_item(const CullLaunch& a, uint32_t item, Wa
   const int nv = (int)min((uint32_t)VPP, sc.n_views - vfirst);
   const uint32_t tile_first = group * kItemTiles;
   const uint32_t n_t = min((uint32_t)kItemTiles, sc.n_tiles - tile_first);
+  // The first tile's transform indices load while the views are staged.
+  const uint4 xf_first = ld_stream4u(sc.soa + 6 * (size_t)sc.cap + tile_first * kTileObjects + (uint32_t)lane * kObjPerThread);
 
   // Stage the views (matrices and output pointers) and their prefilter planes in the
   // warp's shared memory when the view group changes; consecutive items of one scene
@@ -336,8 +342,12 @@ __device__ __forceinline__ void warp_item(const CullLaunch& a, uint32_t item, Wa
   }
 
   uint32_t qn = 0;
-  for (uint32_t t = 0; t < n_t; ++t)
-    qn = classify_tile<VPP, PF>(a, ws, sc, tile_first + t, t, tile_first, nv, qn, lane);
+  uint4 xf = xf_first;
+  for (uint32_t t = 0; t < n_t; ++t) {
+    uint4 xf_next = make_uint4(0u, 0u, 0u, 0u);
+    qn = classify_tile<VPP, PF>(a, ws, sc, tile_first + t, t, tile_first, n_t, nv, qn, lane, xf, xf_next);
+    xf = xf_next;
+  }
   if (PF && qn) drain_queue(ws, sc, tile_first, qn, lane);
   else __syncwarp();
   finish_item<VPP>(ws, tile_first, n_t, nv, lane);

@@ -83,6 +83,7 @@ _SIGS = {
     "dpcull_plan_launch": (_I, [_P, _U32]),
     "dpcull_plan_tuning": (_I, [_P, _U32, C.POINTER(Tuning)]),
     "dpcull_plan_kernel_ms": (_I, [_P, _U32, _U32, C.POINTER(C.c_float)]),
+    "dpcull_plan_read": (_I, [_P, _U32, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
     "dpcull_plan_destroy": (_I, [_P, _U32]),
     "dpcull_autotune": (_I, [_P, C.POINTER(Job), _SZ, C.POINTER(Tuning)]),
     "dpcull_tree_create": (_I, [_P, _SZ, _UP]),
@@ -360,6 +361,17 @@ class Context:
         ms = C.c_float()
         _check(self.lib.dpcull_plan_kernel_ms(self.h, p, back, C.byref(ms)))
         return ms.value
+
+    def plan_read(self, p: int, bits: list, changed: list) -> np.ndarray:
+        """Reads every result of the plan's last launch into the given uint32 arrays (one per
+        result, in job and view order; None skips); returns the changed-list lengths."""
+        n = len(bits)
+        bp = (C.c_void_p * n)(*[(b.ctypes.data if b is not None else None) for b in bits])
+        cp = (C.c_void_p * n)(*[(c.ctypes.data if c is not None else None) for c in changed])
+        caps = (C.c_size_t * n)(*[(c.size if c is not None else 0) for c in changed])
+        out = np.zeros(n, np.uint64)
+        _check(self.lib.dpcull_plan_read(self.h, p, bp, cp, caps, out.ctypes.data))
+        return out
 
     def plan_tuning(self, p: int) -> dict:
         t = Tuning()

@@ -191,14 +191,19 @@ def test_plan_graph_frames(ctx):
     obbs = oracle.build_obbs(sc["lower"], sc["extent"], sc["xform"], sc["mats"])
     n = 300_000
     prev = [np.full((n + 31) // 32, 0xFFFFFFFF, np.uint32) for _ in range(8)]
+    out_bits = [np.zeros((n + 31) // 32, np.uint32) for _ in range(8)]
+    out_changed = [np.zeros(n, np.uint32) for _ in range(8)]
     for vps in frames:
         ctx.plan_set_views(p, vps)
         ctx.plan_launch(p)
+        n_ch = ctx.plan_read(p, out_bits, out_changed)  # every result in two waits
         for v in range(8):
             bits = oracle.cull_obbs(obbs, vps[v], threads=8)
             ch = oracle.update_changed(prev[v], bits, n)
             assert np.array_equal(ctx.result_bits(rs[v]), bits)
             assert np.array_equal(ctx.result_changed(rs[v]), ch)
+            assert np.array_equal(out_bits[v], bits)
+            assert n_ch[v] == len(ch) and np.array_equal(out_changed[v][: len(ch)], ch)
     # a plan without set_views replays its last matrices
     ctx.plan_launch(p)
     for v in range(8):
