@@ -108,29 +108,14 @@ __device__ __forceinline__ void classify_views(WarpShared& ws, const pf::Box (&b
 {
 #pragma unroll 1
   for (int v = 0; v < nv; ++v) {
-    const pf::Planes& P = ws.pl[v];
-    const pf::F4 n01 = P.n01, n2g = P.n2g;
-    float mi[kObjPerThread], mo[kObjPerThread];
-    {
-      const pf::F4 ql = P.q[0][0], qh = P.q[0][1];
-#pragma unroll
-      for (int k = 0; k < kObjPerThread; ++k) pf::axis<true>(bx[k], ql, qh, n01.x, n01.y, mi[k], mo[k]);
-    }
-#pragma unroll
-    for (int ax = 1; ax < 3; ++ax) {
-      const pf::F4 ql = P.q[ax][0], qh = P.q[ax][1];
-      const float nl = ax == 1 ? n01.z : n2g.x;
-      const float nh = ax == 1 ? n01.w : n2g.y;
-#pragma unroll
-      for (int k = 0; k < kObjPerThread; ++k) pf::axis(bx[k], ql, qh, nl, nh, mi[k], mo[k]);
-    }
+    const pf::PlaneRegs P = pf::load_planes(ws.pl[v]);
     uint32_t in = 0, und = 0;
 #pragma unroll
     for (int k = 0; k < kObjPerThread; ++k) {
-      const float d = bx[k].d0 + n2g.z;
-      const bool vis = mi[k] > d, out = mo[k] <= -d;
+      bool vis, inv;
+      pf::decide(bx[k], P, vis, inv);
       in |= (uint32_t)vis << k;
-      und |= (uint32_t)(!vis && !out) << k;
+      und |= (uint32_t)(!vis & !inv) << k;
     }
     // bit k of und -> bit 8k (the multiply places each bit k at 8k; the mask drops the
     // cross terms), then view v's column
@@ -198,7 +183,7 @@ __device__ __forceinline__ uint32_t classify_tile(const CullLaunch& a, WarpShare
     for (int k = 0; k < kObjPerThread; ++k) {
       const uint32_t mi = compu(xf, k);
       const bool exists = obj0 + k < sc.n_objects;
-      const bool use = exists && mi < sc.n_mats;
+      const bool use = exists & (mi < sc.n_mats);
       if (exists && !use && atomicOr(&a.ctl->error, kErrBadTransform) == 0) a.ctl->error_info = obj0 + k;
       float4 r0 = make_float4(0.f, 0.f, 0.f, 0.f), r1 = r0, r2 = r0, r3 = r0;
       if (use) {

@@ -15,47 +15,52 @@
 // (ManagerImpl.cpp:224-227) is set when every corner has it; visible <=> no cfa bit.
 // u = 2^-24.
 //
-// Planes (per view).  Pi_lo = col_a + col_w, Pi_hi = col_w - col_a, B_a[i] = |col_a[i]| +
-// |col_w[i]| (so |Pi_i| <= B_a[i]), Nx_a = ||B_a,xyz||, Bw_a = B_a[w].  The stored plane
-// is Q = fl(fl(Pi) * r), r = fl(1 / Nx'_a) with Nx'_a >= Nx_a; hence Q = r Pi + eps,
-// |eps_i| <= 2.01u r |Pi_i|, r Nx_a <= 1 + u and ||Q_xyz|| <= 1 + 3.1u.  Stored with it:
-// q >= ||Q_xyz|| and, per view, g = delta rho with rho >= max_a Bw_a / Nx'_a.
+// Planes (per view).  For plane k (axis a, side lo/hi): Pi_k = col_a + col_w (lo) or
+// col_w - col_a (hi), B_a[i] = |col_a[i]| + |col_w[i]| (so |Pi_i| <= B_a[i]),
+// Nx_a = ||B_a,xyz||, Bw_a = B_a[w].  The stored plane is Q = fl(fl(Pi) * r_k) with
+// r_k = fl(1 / n_k); hence Q = r_k Pi + eps, |eps_i| <= 2.01u r_k |Pi_i|.  The five planes
+// other than z-hi (class A) use n_k >= ||Pi_k,xyz||, so ||Q_xyz|| <= 1 + 3.1u; the z-hi
+// plane (class B: the far plane of a perspective view, often nearly pure w) uses
+// n_k >= Nx_z and keeps q >= ||Q_xyz|| (<= 1 + 3.1u).  Per class, kappa >= r_k Nx_a and
+// rho >= r_k Bw_a (the largest over the class's planes) give the margin terms below.
 //
 // Box (per object).  Only affine world matrices (column w = (0, 0, 0, 1), every matrix
 // of the reference's scene graph) are bounded; a box with a projective matrix gets a NaN
 // margin and all its pairs take the exact test.  Then X_w = Y_w = Z_w = 0 and p_w = 1.
 // b_j = sum_i (|l_i| + |e_i|) |M_ij| + |M_3j| bounds every magnitude involved
 // (|p_j| + |X_j| + |Y_j| + |Z_j| <= (1 + 5.01u) b_j); Bxyz >= ||b_xyz|| and b_w = 1.  For
-// every axis, with S_a = sum_j b_j B_a[j]: r S_a <= r (Bxyz Nx_a + Bw_a) <= (1 + u) Bxyz +
+// plane k, with S_a = sum_j b_j B_a[j]: r_k S_a <= r_k (Bxyz Nx_a + Bw_a) <= Bxyz kappa +
 // rho (Cauchy-Schwarz on xyz only: the view's translation row lives in w, apart from the
 // objects' xyz magnitudes).  The centre K = p + (X + Y + Z) / 2 is the mean of the 8
 // corners.  We compute c~ = (l + e/2) * M with FMAs (c~_w = 1 exactly): |c~_j - K_j| <=
 // 9.7u b_j.  R >= (||X_xyz|| + ||Y_xyz|| + ||Z_xyz||) / 2, so for every corner C_s.Q lies
-// in K.Q +- E with E = R q (|X.Q| <= ||X_xyz|| ||Q_xyz|| as X_w = 0).
+// in K.Q +- E with E = R q (|X.Q| <= ||X_xyz|| ||Q_xyz|| as X_w = 0); the stored radius
+// r' = R (1 + 2^-18) >= E / (1 - u) for every class-A plane (q <= 1 + 3.1u).
 //
-// Errors, in the plane's units (all of the form u r S_a):
+// Errors, in the plane's units (all of the form u r_k S_a):
 //   |r (c_a + c_w)_s - r C_s.Pi| <= 7.04u r S_a   (the reference's dot products and add
 //                                                  chain, 7u sum_j a_j B_a[j]),
 //   |C_s.eps| <= 2.02u r S_a,
 //   |L - K.Q| <= 13.75u r S_a   (L = fl(c~.Q), an FMA chain: 9.72u + 4.02u),
-// so every r (c_a + c_w)_s (and the hi analogue c_w - c_a) is within 22.9u (Bxyz + rho) of
-// the real value that L and E describe.  The margin is D = d0 + g with d0 = delta Bxyz +
-// eta per box and g = delta rho per view, delta = 2^-19 = 32u, which also absorbs the
-// roundings of D and of t = fl(L + E), s = fl(L - E) (each a relative u of the tested
-// quantity); eta = 2^-120 absorbs subnormal rounding.
+// so every r (c_a + c_w)_s (and the hi analogue c_w - c_a) is within
+// 22.9u (Bxyz kappa + rho) of the real value that L and E describe.  The margins are
+// D = d0 kappa + g per class with d0 = delta Bxyz + eta per box and g = delta rho per view,
+// delta = 2^-19 = 32u, which also absorbs the roundings of D and of the thresholds below
+// (each a relative u of the tested quantity); eta = 2^-120 absorbs subnormal rounding.
 //
-// Decisions (for one view):
-//   * visible   if L > D for all six planes: the corner mean K is inside every plane, so
-//     for each plane some corner has a strictly positive rounded value and no cfa bit can
-//     be set;
-//   * invisible if for some axis t_lo = fl(L_lo + E_lo) <= -D (every corner passes the lo
-//     test), or t_hi <= -D and s_lo = fl(L_lo - E_lo) >= D (every corner fails the lo
-//     test and passes the hi test);
+// Decisions (for one view; T_A = fl(D_A + r'), u = fl(L_zhi + R q)):
+//   * visible   if L > D_A for the class-A planes and L_zhi > D_B: the corner mean K is
+//     inside every plane, so for each plane some corner has a strictly positive rounded
+//     value and no cfa bit can be set;
+//   * invisible if some lo plane has L <= -T_A (every corner passes the lo test), or the
+//     x-hi / y-hi plane has L <= -T_A while its lo plane has L >= T_A (every corner fails
+//     the lo test and passes the hi test), or u <= -D_B while the z-lo plane has
+//     L >= T_A;
 //   * otherwise undecided.
 // The bounds need finite values without overflow: a box whose Bxyz is not below 2^50 (or
-// is NaN) gets d0 = NaN, and a view whose entries are not finite, whose Nx'_a is not in
-// [2^-60, 2^50) or whose rho is not below 2^50 gets g = NaN; every pair of either is
-// undecided (no comparison with a NaN margin holds).
+// is NaN) gets d0 = NaN, and a view whose entries are not finite, whose plane or axis
+// norms are not in [2^-60, 2^50) or whose kappa or rho is not below 2^50 gets NaN
+// margins; every pair of either is undecided (no comparison with a NaN margin holds).
 #pragma once
 
 #include <cmath>
@@ -107,13 +112,11 @@ DPCULL_HD float bound_norm(float x, float y, float z, float w = 0.f)
   return std::sqrt(std::fma(x, x, std::fma(y, y, std::fma(z, z, w * w)))) * kInflate;
 }
 
-// Prefilter planes of one view (128 bytes, staged in shared memory by the cull).
+// Prefilter planes of one view (112 bytes, staged in shared memory by the cull).
 struct Planes {
-  F4 q[3][2];  // axis a: lo plane Q_lo, hi plane Q_hi
-  F4 n01;      // (q_lo, q_hi) of axes x and y
-  F4 n2g;      // (q_lo, q_hi) of axis z, then g (NaN when the view cannot be bounded), 0
-  DPCULL_HD float qlo(int a) const { return a == 0 ? n01.x : a == 1 ? n01.z : n2g.x; }
-  DPCULL_HD float qhi(int a) const { return a == 0 ? n01.y : a == 1 ? n01.w : n2g.y; }
+  F4 q[3][2];  // axis a: lo plane, hi plane
+  F4 m;        // (kappa_A, g_A, kappa_B, g_B); the g are NaN when the view cannot be bounded
+  F4 qf;       // (q of the z-hi plane, 0, 0, 0)
 };
 
 // Builds the planes of a row-major Mat44f view-projection; false when the view cannot be
@@ -122,36 +125,46 @@ DPCULL_HD bool make_planes(const float* vp, Planes& out)
 {
   bool ok = true;
   for (int i = 0; i < 16; ++i) ok = ok && std::isfinite(vp[i]);
-  float rho = 0.f, qn[3][2];
+  float kA = 0.f, rA = 0.f, kB = 0.f, rB = 0.f, qf = 0.f;
   for (int a = 0; a < 3; ++a) {
-    float B[4], lo[4], hi[4];
+    float B[4], pl[2][4];
     for (int i = 0; i < 4; ++i) {
       const float ca = vp[4 * i + a], cw = vp[4 * i + 3];
       B[i] = std::fabs(ca) + std::fabs(cw);
-      lo[i] = ca + cw;
-      hi[i] = cw - ca;
+      pl[0][i] = ca + cw;
+      pl[1][i] = cw - ca;
     }
     const float nx = bound_norm(B[0], B[1], B[2]) * kInflate;
     ok = ok && nx < kLimit && nx >= kTiny;
-    const float r = ok ? 1.0f / nx : 0.f;
-    rho = std::fmax(rho, B[3] * r * kInflate);
-    const F4 ql = {lo[0] * r, lo[1] * r, lo[2] * r, lo[3] * r};
-    const F4 qh = {hi[0] * r, hi[1] * r, hi[2] * r, hi[3] * r};
-    out.q[a][0] = ql;
-    out.q[a][1] = qh;
-    qn[a][0] = bound_norm(ql.x, ql.y, ql.z) * kInflate;
-    qn[a][1] = bound_norm(qh.x, qh.y, qh.z) * kInflate;
+    for (int h = 0; h < 2; ++h) {
+      const bool far = a == 2 && h == 1;
+      const float n = far ? nx : bound_norm(pl[h][0], pl[h][1], pl[h][2]) * kInflate;
+      ok = ok && n < kLimit && n >= kTiny;
+      const float r = ok ? 1.0f / n : 0.f;
+      const F4 q = {pl[h][0] * r, pl[h][1] * r, pl[h][2] * r, pl[h][3] * r};
+      out.q[a][h] = q;
+      const float kap = nx * r * kInflate, rho = B[3] * r * kInflate;
+      if (far) {
+        kB = kap;
+        rB = rho;
+        qf = bound_norm(q.x, q.y, q.z) * kInflate;
+      } else {
+        kA = std::fmax(kA, kap);
+        rA = std::fmax(rA, rho);
+      }
+    }
   }
-  ok = ok && rho < kLimit;
+  ok = ok && kA < kLimit && rA < kLimit && kB < kLimit && rB < kLimit;
   // A NaN g makes every margin of the view NaN: no comparison holds, nothing is decided.
-  const float g = ok ? kDelta * rho * kInflate : nan_value();
-  out.n01 = F4{qn[0][0], qn[0][1], qn[1][0], qn[1][1]};
-  out.n2g = F4{qn[2][0], qn[2][1], g, 0.f};
+  const float nan = nan_value();
+  out.m = F4{kA, ok ? kDelta * rA * kInflate : nan, kB, ok ? kDelta * rB * kInflate : nan};
+  out.qf = F4{qf, 0.f, 0.f, 0.f};
   return ok;
 }
 
-// Prefilter box of one object: centre c (c.w == 1), extent bound R and margin d0 (NaN
-// when the bounds do not apply, including every box with a projective world matrix).
+// Prefilter box of one object: centre c (c.w == 1), radius r' = R (1 + 2^-18) and margin
+// d0 (NaN when the bounds do not apply, including every box with a projective world
+// matrix).
 struct Box {
   float cx, cy, cz;
   float r, d0;
@@ -181,7 +194,7 @@ DPCULL_HD float row_norm(const F4& m)
 // True when the matrix maps w = 1 to w = 1 and directions to w = 0 (no projective part).
 DPCULL_HD bool is_affine(const F4& m0, const F4& m1, const F4& m2, const F4& m3)
 {
-  return m0.w == 0.f && m1.w == 0.f && m2.w == 0.f && m3.w == 1.f;
+  return (m0.w == 0.f) & (m1.w == 0.f) & (m2.w == 0.f) & (m3.w == 1.f);  // no branches
 }
 
 DPCULL_HD Box make_box(float lx, float ly, float lz, float ex, float ey, float ez, const F4& m0,
@@ -194,49 +207,57 @@ DPCULL_HD Box make_box(float lx, float ly, float lz, float ex, float ey, float e
   b.cz = std::fma(cz0, m2.z, std::fma(cy0, m1.z, std::fma(cx0, m0.z, m3.z)));
   const float n0 = row_norm(m0), n1 = row_norm(m1), n2 = row_norm(m2);
   const float aex = std::fabs(ex), aey = std::fabs(ey), aez = std::fabs(ez);
-  b.r = 0.5f * kInflate * (aex * n0 + aey * n1 + aez * n2);
+  b.r = 0.5f * kInflate * (aex * n0 + aey * n1 + aez * n2) * kInflate;
   const float sx = std::fabs(lx) + aex, sy = std::fabs(ly) + aey, sz = std::fabs(lz) + aez;
   const float bxyz = kInflate * (sx * n0 + sy * n1 + sz * n2 +
                                  (std::fabs(m3.x) + std::fabs(m3.y) + std::fabs(m3.z)));
-  b.d0 = (bxyz < kLimit && is_affine(m0, m1, m2, m3)) ? std::fma(kDelta, bxyz, kEta) : nan_value();
+  b.d0 = ((bxyz < kLimit) & is_affine(m0, m1, m2, m3)) ? std::fma(kDelta, bxyz, kEta) : nan_value();
   return b;
 }
 
-// One axis of one view for one box: folds the axis's planes into the running minima
-//   mi = min over planes of L (the visible test), mo = min over axes of the invisible
-//   candidate min(t_lo, max(t_hi, -s_lo)).
-// c.w == 1: Q_w is the addend of L; E = R q, and t = fl(L + R q), s = fl(L - R q) are one
-// rounding each.
-template <bool kFirst = false>
-DPCULL_HD void axis(const Box& b, const F4& ql, const F4& qh, float nl, float nh, float& mi,
-                    float& mo)
+// Plane value L = c.Q (c.w == 1: Q_w is the addend).
+DPCULL_HD float plane(const Box& b, const F4& q)
 {
-  const float Ll = std::fma(b.cz, ql.z, std::fma(b.cy, ql.y, std::fma(b.cx, ql.x, ql.w)));
-  const float Lh = std::fma(b.cz, qh.z, std::fma(b.cy, qh.y, std::fma(b.cx, qh.x, qh.w)));
-  const float tl = std::fma(b.r, nl, Ll), sl = std::fma(-b.r, nl, Ll);
-  const float th = std::fma(b.r, nh, Lh);
-  if (kFirst) {  // the first axis starts the minima
-    mo = std::fmin(tl, std::fmax(th, -sl));
-    mi = std::fmin(Ll, Lh);
-  } else {
-    mo = std::fmin(mo, std::fmin(tl, std::fmax(th, -sl)));
-    mi = std::fmin(mi, std::fmin(Ll, Lh));
-  }
+  return std::fma(b.cz, q.z, std::fma(b.cy, q.y, std::fma(b.cx, q.x, q.w)));
+}
+
+// A view's planes in registers, read once for several boxes.
+struct PlaneRegs {
+  F4 xl, xh, yl, yh, zl, zh, m;
+  float qf;
+};
+
+DPCULL_HD PlaneRegs load_planes(const Planes& p)
+{
+  return PlaneRegs{p.q[0][0], p.q[0][1], p.q[1][0], p.q[1][1], p.q[2][0], p.q[2][1], p.m, p.qf.x};
+}
+
+// The decisions of the comment at the top for one box in one view.
+DPCULL_HD void decide(const Box& b, const PlaneRegs& p, bool& visible, bool& invisible)
+{
+  const float xl = plane(b, p.xl), xh = plane(b, p.xh);
+  const float yl = plane(b, p.yl), yh = plane(b, p.yh);
+  const float zl = plane(b, p.zl), zh = plane(b, p.zh);
+  const float da = std::fma(b.d0, p.m.x, p.m.y), db = std::fma(b.d0, p.m.z, p.m.w);
+  const float ta = da + b.r;
+  const float uf = std::fma(b.r, p.qf, zh);
+  const float mlo = std::fmin(std::fmin(xl, yl), zl);
+  const float min_in = std::fmin(std::fmin(mlo, xh), yh);
+  const float o = std::fmin(mlo, std::fmin(std::fmax(xh, -xl), std::fmax(yh, -yl)));
+  // bitwise, not short-circuit: no branches in the kernels
+  visible = (min_in > da) & (zh > db);
+  invisible = (o <= -ta) | ((uf <= -db) & (zl >= ta));
 }
 
 enum : int { kInvisible = 0, kVisible = 1, kUndecided = 2 };
 
-// Whole classification of one box in one view (the kernels inline the same steps, with
-// the view's planes shared by several boxes).
+// Whole classification of one box in one view (the kernels run decide() with the view's
+// planes loaded once for several boxes).
 DPCULL_HD int classify(const Box& b, const Planes& p)
 {
-  const float d = b.d0 + p.n2g.z;
-  float mi, mo;
-  axis<true>(b, p.q[0][0], p.q[0][1], p.qlo(0), p.qhi(0), mi, mo);
-  for (int a = 1; a < 3; ++a) axis(b, p.q[a][0], p.q[a][1], p.qlo(a), p.qhi(a), mi, mo);
-  if (mi > d) return kVisible;
-  if (mo <= -d) return kInvisible;
-  return kUndecided;
+  bool vis, inv;
+  decide(b, load_planes(p), vis, inv);
+  return vis ? kVisible : inv ? kInvisible : kUndecided;
 }
 
 }  // namespace pf

@@ -16,6 +16,7 @@ waits for the arrival time and calls dpcull_server_submit.
 from __future__ import annotations
 
 import ctypes as C
+import gc
 import math
 import time
 
@@ -120,6 +121,8 @@ def run_load(server: native.Server, times, scenes, nviews, vps, warmup_s: float 
     m = len(times)
     ids = np.zeros(m, np.uint64)
     done = []
+    gc_was_on = gc.isenabled()
+    gc.disable()  # no collector pauses inside the submission loop
     t0 = time.perf_counter()
     clock0 = server.now()
     late = 0
@@ -139,6 +142,8 @@ def run_load(server: native.Server, times, scenes, nviews, vps, warmup_s: float 
         ids[i] = rid.value
     server.drain()
     wall = time.perf_counter() - t0
+    if gc_was_on:
+        gc.enable()
     done.append(server.poll_array())
     comp = np.concatenate(done)
     # request ids are consecutive in submission order
