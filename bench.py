@@ -525,7 +525,8 @@ def run_serving(ctx, args) -> dict:
                 "warmup_s": args.serve_warmup, "evictions": st["scene_evictions"],
                 "uploads": st["scene_uploads"], "upload_gb": st["upload_bytes"] / 1e9,
                 "batches": st["batches"], "max_batch_requests": st["max_batch_requests"],
-                "streams": 3})
+                "streams": 3, "scheduler": {k: st[k] for k in ("max_turn_us", "slow_turns",
+                                                               "max_upload_call_us", "max_evict_call_us")}})
     return res
 
 

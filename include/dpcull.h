@@ -250,6 +250,8 @@ typedef struct dpcull_server_stats {
   uint64_t scene_uploads, scene_evictions, upload_bytes;
   uint64_t resident_bytes, resident_scenes, budget_bytes;
   uint64_t max_batch_requests, pending_requests;
+  /* scheduler timing: longest turn, turns over 1 ms, longest upload / eviction call (us) */
+  uint64_t max_turn_us, slow_turns, max_upload_call_us, max_evict_call_us;
 } dpcull_server_stats;
 
 /* Steady-clock seconds; the clock of dpcull_completion's timestamps. */

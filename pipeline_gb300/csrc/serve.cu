@@ -149,8 +149,11 @@ int vpp_for(uint32_t max_views)
   return max_views <= 1 ? 1 : max_views <= 2 ? 2 : max_views <= 4 ? 4 : 8;
 }
 
+uint64_t us_since(double t0) { return (uint64_t)((now_s() - t0) * 1e6); }
+
 void evict(dpcull_server s, Scene& sc)
 {
+  const double t0 = now_s();
   // Every batch that read the scene has retired (pending == 0), so its memory is free to
   // go back to the pool in upload-stream order.
   cudaFreeAsync(sc.dev, s->up_stream);
@@ -159,6 +162,7 @@ void evict(dpcull_server s, Scene& sc)
   s->lru.erase(sc.lru);
   s->resident_bytes -= sc.bytes;
   s->stats.scene_evictions++;
+  s->stats.max_evict_call_us = std::max(s->stats.max_evict_call_us, us_since(t0));
 }
 
 // Makes room for `need` more bytes, evicting least recently used idle scenes.  With
@@ -190,6 +194,7 @@ bool make_room(dpcull_server s, uint64_t need, bool take_uploaded)
 // Starts the upload of a scene on the upload stream (one copy from its pinned image).
 void upload(dpcull_server s, Scene& sc, uint32_t id)
 {
+  const double t0 = now_s();
   cudaMallocAsync((void**)&sc.dev, sc.bytes, s->up_stream);
   cudaMemcpyAsync(sc.dev, sc.packed, sc.bytes, cudaMemcpyHostToDevice, s->up_stream);
   if (!sc.ready) cudaEventCreateWithFlags(&sc.ready, cudaEventDisableTiming);
@@ -201,6 +206,7 @@ void upload(dpcull_server s, Scene& sc, uint32_t id)
   s->resident_bytes += sc.bytes;
   s->stats.scene_uploads++;
   s->stats.upload_bytes += sc.bytes;
+  s->stats.max_upload_call_us = std::max(s->stats.max_upload_call_us, us_since(t0));
 }
 
 void retire(dpcull_server s, Slot& slot)
@@ -257,9 +263,26 @@ void copy_kept(Slot& slot)
   }
 }
 
+// Starts the uploads of scenes that requests found missing (after the turn's batch went
+// out, so no hit waits on these calls).  At most half the budget is in uploads that no
+// batch has taken yet (any one scene may upload alone).
+void start_uploads(dpcull_server s, const std::vector<uint32_t>& missing)
+{
+  if (missing.empty()) return;
+  std::lock_guard<std::mutex> lk(s->scenes_mu);
+  for (uint32_t id : missing) {
+    Scene& sc = s->scenes[id];
+    if (sc.resident) continue;  // two requests of this turn wanted it
+    if ((s->uploading_bytes == 0 || s->uploading_bytes + sc.bytes <= s->budget / 2) &&
+        make_room(s, sc.bytes, false))
+      upload(s, sc, id);
+  }
+}
+
 bool launch(dpcull_server s, Slot& slot)
 {
   std::vector<Request> take;
+  std::vector<uint32_t> missing;
   uint64_t work = 0, out_bytes = 0;
   uint32_t max_views = 1;
   // Take the pending requests out under the lock, decide outside it (submitters never
@@ -275,15 +298,11 @@ bool launch(dpcull_server s, Slot& slot)
     bool full = false;
     for (auto& q : cand) {
       Scene& sc = s->scenes[q.scene];
-      // A scene that is not on the device yet starts its upload now and its requests wait
-      // in the queue; the batch goes ahead with the scenes that are ready, so a miss never
-      // holds up the hits of the same batch.
-      // At most half the budget is in uploads that no batch has taken yet (any one scene
-      // may upload alone).
+      // A scene that is not on the device yet gets its upload started after this turn's
+      // batch and its requests wait in the queue; the batch goes ahead with the scenes
+      // that are ready, so a miss never holds up the hits of the same batch.
       if (!sc.resident) {
-        if ((s->uploading_bytes == 0 || s->uploading_bytes + sc.bytes <= s->budget / 2) &&
-            make_room(s, sc.bytes, false))
-          upload(s, sc, q.scene);
+        missing.push_back(q.scene);
         left.push_back(q);
         continue;
       }
@@ -323,7 +342,10 @@ bool launch(dpcull_server s, Slot& slot)
     std::lock_guard<std::mutex> lk(s->pending_mu);
     s->pending.insert(s->pending.begin(), left.begin(), left.end());
   }
-  if (take.empty()) return false;
+  if (take.empty()) {
+    start_uploads(s, missing);
+    return false;
+  }
 
   // Every scene of the batch was seen uploaded (its event complete) before admission.
   size_t n_views = 0;
@@ -414,6 +436,7 @@ bool launch(dpcull_server s, Slot& slot)
   s->stats.batches++;
   s->stats.max_batch_requests = std::max<uint64_t>(s->stats.max_batch_requests, slot.reqs.size());
   if (cudaGetLastError() != cudaSuccess) s->error = DPCULL_ERR_CUDA;
+  start_uploads(s, missing);
   return true;
 }
 
@@ -421,6 +444,7 @@ void worker_main(dpcull_server s)
 {
   cudaSetDevice(s->device);
   while (!s->stop.load()) {
+    const double turn0 = now_s();
     bool progress = false;
     for (uint32_t i = 0; i < s->n_streams; ++i) {
       Slot& slot = s->slots[i];
@@ -442,6 +466,9 @@ void worker_main(dpcull_server s)
         break;  // at most one new batch per turn, so that arrivals can join the next one
       }
     }
+    const uint64_t turn_us = us_since(turn0);
+    s->stats.max_turn_us = std::max(s->stats.max_turn_us, turn_us);
+    if (turn_us > 1000) s->stats.slow_turns++;
     if (!progress) {
       bool busy = false;
       for (uint32_t i = 0; i < s->n_streams; ++i) busy |= s->slots[i].busy;
@@ -476,6 +503,15 @@ int dpcull_server_create(dpcull_ctx ctx, uint64_t budget_bytes, uint32_t n_strea
   if (cudaDeviceGetDefaultMemPool(&pool, s->device) == cudaSuccess) {
     uint64_t keep = ~0ull;  // keep freed blocks for reuse instead of returning them
     cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &keep);
+    // Map the budget into the pool now (allocate and free it once), so that uploads
+    // never wait for the pool to grow while requests are being served.  Best effort:
+    // without the memory the pool grows on demand.
+    void* reserve = nullptr;
+    if (cudaMallocAsync(&reserve, budget_bytes, 0) == cudaSuccess) {
+      cudaFreeAsync(reserve, 0);
+      cudaStreamSynchronize(0);
+    }
+    cudaGetLastError();
   }
   if (cudaStreamCreateWithFlags(&s->up_stream, cudaStreamNonBlocking) != cudaSuccess) {
     cudaGetLastError();

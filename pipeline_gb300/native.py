@@ -124,7 +124,7 @@ class ServerStats(C.Structure):
     _fields_ = [(name, C.c_uint64) for name in (
         "requests_submitted", "requests_completed", "batches", "scene_uploads", "scene_evictions",
         "upload_bytes", "resident_bytes", "resident_scenes", "budget_bytes", "max_batch_requests",
-        "pending_requests")]
+        "pending_requests", "max_turn_us", "slow_turns", "max_upload_call_us", "max_evict_call_us")]
 
     def as_dict(self) -> dict:
         return {name: int(getattr(self, name)) for name, _ in self._fields_}
