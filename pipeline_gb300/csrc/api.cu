@@ -130,6 +130,7 @@ struct Plan {
   int next = 0;
   dpcull_tuning tuning{};
   uint32_t n_items = 0;
+  uint32_t item_tiles = kItemTiles;
   int grid = 0;
 };
 
@@ -422,7 +423,8 @@ int default_vpp(uint32_t max_views)
 // Builds scenes/views for a job list; returns n_items.
 int build_batch(dpcull_ctx c, const dpcull_job* jobs, size_t n_jobs, uint32_t vpp,
                 std::vector<CullScene>& scenes, std::vector<CullView>& views, uint32_t* n_items,
-                std::vector<uint32_t>* groups_out, std::vector<uint32_t>* results_out)
+                std::vector<uint32_t>* groups_out, std::vector<uint32_t>* results_out,
+                uint32_t* item_tiles_out)
 {
   scenes.clear();
   views.clear();
@@ -453,12 +455,19 @@ int build_batch(dpcull_ctx c, const dpcull_job* jobs, size_t n_jobs, uint32_t vp
       views.push_back(view_of(*r, jobs[j].vps + 16 * (size_t)v));
       if (results_out) results_out->push_back(jobs[j].results[v]);
     }
-    CullScene s = scene_of(*g, vb, jobs[j].n_views, vpp, items);
-    items += items_of(s.n_tiles, s.n_vgroups);
+    CullScene s = scene_of(*g, vb, jobs[j].n_views, vpp, 0);
     scenes.push_back(s);
     if (groups_out) groups_out->push_back(jobs[j].group);
   }
+  uint64_t tile_groups = 0;
+  for (auto& s : scenes) tile_groups += (uint64_t)s.n_tiles * s.n_vgroups;
+  const uint32_t it = item_tiles_for(tile_groups, c->sm_count);
+  for (auto& s : scenes) {
+    s.item_begin = items;
+    items += items_of(s.n_tiles, s.n_vgroups, it);
+  }
   *n_items = items;
+  if (item_tiles_out) *item_tiles_out = it;
   return DPCULL_OK;
 }
 
@@ -478,8 +487,8 @@ int persistent_grid(dpcull_ctx c, uint32_t vpp, uint32_t ctas_per_sm, uint32_t n
 // inside a stream capture they become event-record nodes visible outside the graph.
 int launch_batch(dpcull_ctx c, const CullScene* d_scenes, const CullView* d_views,
                  uint32_t n_scenes, uint32_t n_views, uint32_t max_words, uint32_t n_items,
-                 const dpcull_tuning& t, cudaStream_t s, cudaEvent_t k0 = nullptr,
-                 cudaEvent_t k1 = nullptr)
+                 uint32_t item_tiles, const dpcull_tuning& t, cudaStream_t s,
+                 cudaEvent_t k0 = nullptr, cudaEvent_t k1 = nullptr)
 {
   if (n_views > 65535) return fail(DPCULL_ERR_INVALID_ARGUMENT, "at most 65535 views per launch");
   CullLaunch a{};
@@ -487,6 +496,7 @@ int launch_batch(dpcull_ctx c, const CullScene* d_scenes, const CullView* d_view
   a.views = d_views;
   a.n_scenes = n_scenes;
   a.n_items = n_items;
+  a.item_tiles = item_tiles;
   a.items_per_ticket = std::max<uint32_t>(1, t.tiles_per_ticket);
   a.exact_only = c->exact_only ? 1u : 0u;
   a.ctl = c->ctl;
@@ -966,7 +976,8 @@ int dpcull_cull(dpcull_ctx c, dpcull_group gh, dpcull_result rh, const float vp[
   a.ctl = c->ctl;
   a.one_scene = scene_of(*g, 0, 1, 1, 0);
   a.one_view = view_of(*r, vp);
-  a.n_items = items_of(a.one_scene.n_tiles, 1);
+  a.item_tiles = item_tiles_for(a.one_scene.n_tiles, c->sm_count);
+  a.n_items = items_of(a.one_scene.n_tiles, 1, a.item_tiles);
   const int grid = persistent_grid(c, 1, 0, a.n_items, 1);
   if (launch_cull(a, grid, 1, c->stream)) return cuda_fail(cudaGetLastError(), "cull launch");
   if (launch_changed_lists(nullptr, a.one_view, 1, a.one_view.n_words, c->stream))
@@ -1059,8 +1070,8 @@ int dpcull_cull_batched(dpcull_ctx c, const dpcull_job* jobs, size_t n_jobs, con
   if (!valid_vpp(t.views_per_pass)) return fail(DPCULL_ERR_INVALID_ARGUMENT, "views_per_pass must be 1, 2, 4 or 8");
   std::vector<CullScene> scenes;
   std::vector<CullView> views;
-  uint32_t items = 0;
-  int rc = build_batch(c, jobs, n_jobs, t.views_per_pass, scenes, views, &items, nullptr, nullptr);
+  uint32_t items = 0, item_tiles = kItemTiles;
+  int rc = build_batch(c, jobs, n_jobs, t.views_per_pass, scenes, views, &items, nullptr, nullptr, &item_tiles);
   if (rc) return rc;
   if (!items) return DPCULL_OK;
   CullScene* ds = nullptr;
@@ -1075,7 +1086,7 @@ int dpcull_cull_batched(dpcull_ctx c, const dpcull_job* jobs, size_t n_jobs, con
   cudaMemcpyAsync(ds, scenes.data(), scenes.size() * sizeof(CullScene), cudaMemcpyHostToDevice, c->stream);
   cudaMemcpyAsync(dv, views.data(), views.size() * sizeof(CullView), cudaMemcpyHostToDevice, c->stream);
   rc = launch_batch(c, ds, dv, (uint32_t)scenes.size(), (uint32_t)views.size(), max_words_of(scenes),
-                    items, t, c->stream);
+                    items, item_tiles, t, c->stream);
   cudaStreamSynchronize(c->stream);
   dfree(c, ds, scenes.size() * sizeof(CullScene));
   dfree(c, dv, views.size() * sizeof(CullView));
@@ -1095,7 +1106,8 @@ static int plan_capture(dpcull_ctx c, Plan& p, int slot)
   if (e == cudaSuccess) {
     const uint64_t before = c->launches;
     rc = launch_batch(c, p.d_scenes, p.d_views, (uint32_t)p.scenes.size(), (uint32_t)p.views.size(),
-                      max_words_of(p.scenes), p.n_items, p.tuning, cs, p.kt[slot][0], p.kt[slot][1]);
+                      max_words_of(p.scenes), p.n_items, p.item_tiles, p.tuning, cs, p.kt[slot][0],
+                      p.kt[slot][1]);
     c->launches = before;  // counted when the graph is replayed
   }
   cudaError_t e2 = cudaStreamEndCapture(cs, &graph);
@@ -1110,15 +1122,15 @@ static int plan_capture(dpcull_ctx c, Plan& p, int slot)
 
 static int time_batch(dpcull_ctx c, const CullScene* ds, const CullView* dv,
                       const std::vector<CullScene>& sc, const std::vector<CullView>& vw,
-                      uint32_t items, const dpcull_tuning& t, int reps, float* ms)
+                      uint32_t items, uint32_t item_tiles, const dpcull_tuning& t, int reps, float* ms)
 {
   cudaEvent_t e0, e1;
   CU(cudaEventCreate(&e0));
   CU(cudaEventCreate(&e1));
   const uint32_t ns = (uint32_t)sc.size(), nvw = (uint32_t)vw.size(), mt = max_words_of(sc);
-  int rc = launch_batch(c, ds, dv, ns, nvw, mt, items, t, c->stream);  // warm-up
+  int rc = launch_batch(c, ds, dv, ns, nvw, mt, items, item_tiles, t, c->stream);  // warm-up
   if (!rc) cudaEventRecord(e0, c->stream);
-  for (int i = 0; i < reps && !rc; ++i) rc = launch_batch(c, ds, dv, ns, nvw, mt, items, t, c->stream);
+  for (int i = 0; i < reps && !rc; ++i) rc = launch_batch(c, ds, dv, ns, nvw, mt, items, item_tiles, t, c->stream);
   if (!rc) {
     cudaEventRecord(e1, c->stream);
     cudaEventSynchronize(e1);
@@ -1140,7 +1152,7 @@ int dpcull_autotune(dpcull_ctx c, const dpcull_job* jobs, size_t n_jobs, dpcull_
   std::vector<CullScene> scenes;
   std::vector<CullView> views;
   uint32_t items = 0;
-  int rc = build_batch(c, jobs, n_jobs, 1, scenes, views, &items, nullptr, nullptr);
+  int rc = build_batch(c, jobs, n_jobs, 1, scenes, views, &items, nullptr, nullptr, nullptr);
   if (rc) return rc;
   const std::string key = tune_key(scenes, views);
   auto it = c->tune_cache.find(key);
@@ -1164,8 +1176,8 @@ int dpcull_autotune(dpcull_ctx c, const dpcull_job* jobs, size_t n_jobs, dpcull_
     if (vpp > 1 && vpp / 2 >= maxv) continue;  // wider passes than any scene has views
     std::vector<CullScene> sc;
     std::vector<CullView> vw;
-    uint32_t it_items = 0;
-    rc = build_batch(c, jobs, n_jobs, vpp, sc, vw, &it_items, nullptr, nullptr);
+    uint32_t it_items = 0, it_tiles = kItemTiles;
+    rc = build_batch(c, jobs, n_jobs, vpp, sc, vw, &it_items, nullptr, nullptr, &it_tiles);
     if (rc || !it_items) break;
     CullScene* ds = nullptr;
     CullView* dv = nullptr;
@@ -1180,7 +1192,7 @@ int dpcull_autotune(dpcull_ctx c, const dpcull_job* jobs, size_t n_jobs, dpcull_
       for (int cps = 1; cps <= occ; ++cps) {
         dpcull_tuning t{vpp, tpt, (uint32_t)cps, 0};
         float ms = 0;
-        rc = time_batch(c, ds, dv, sc, vw, it_items, t, 3, &ms);
+        rc = time_batch(c, ds, dv, sc, vw, it_items, it_tiles, t, 3, &ms);
         if (rc) break;
         if (ms < best_ms) {
           best_ms = ms;
@@ -1223,7 +1235,8 @@ int dpcull_plan_create(dpcull_ctx c, const dpcull_job* jobs, size_t n_jobs,
   Plan p;
   p.alive = true;
   p.tuning = t;
-  int rc = build_batch(c, jobs, n_jobs, t.views_per_pass, p.scenes, p.views, &p.n_items, &p.groups, &p.results);
+  int rc = build_batch(c, jobs, n_jobs, t.views_per_pass, p.scenes, p.views, &p.n_items, &p.groups, &p.results,
+                       &p.item_tiles);
   if (rc) return rc;
   if (!p.n_items) return fail(DPCULL_ERR_STATE, "plan has no work (all groups empty)");
   for (uint32_t g : p.groups) p.incarnations.push_back(c->groups[g].incarnation);

@@ -295,7 +295,7 @@ __device__ __forceinline__ void warp_item(const CullLaunch& a, uint32_t item, Wa
   const int lane = threadIdx.x & 31;
   __syncwarp();  // the previous item's reads of the shared state are done
   if ((uint64_t)(item - ws.sc.item_begin) >=
-      (uint64_t)((ws.sc.n_tiles + kItemTiles - 1) / kItemTiles) * ws.sc.n_vgroups) {
+      (uint64_t)items_of(ws.sc.n_tiles, ws.sc.n_vgroups, a.item_tiles)) {
     const CullScene* src = a.scenes ? a.scenes + find_scene(a.scenes, a.n_scenes, item) : &a.one_scene;
     constexpr int kSceneWords = (int)(sizeof(CullScene) / 4);
     if (lane < kSceneWords) reinterpret_cast<uint32_t*>(&ws.sc)[lane] = reinterpret_cast<const uint32_t*>(src)[lane];
@@ -306,8 +306,8 @@ __device__ __forceinline__ void warp_item(const CullLaunch& a, uint32_t item, Wa
   const uint32_t group = local / sc.n_vgroups;
   const uint32_t vfirst = (local - group * sc.n_vgroups) * VPP;
   const int nv = (int)min((uint32_t)VPP, sc.n_views - vfirst);
-  const uint32_t tile_first = group * kItemTiles;
-  const uint32_t n_t = min((uint32_t)kItemTiles, sc.n_tiles - tile_first);
+  const uint32_t tile_first = group * a.item_tiles;
+  const uint32_t n_t = min(a.item_tiles, sc.n_tiles - tile_first);
   // The first tile's transform indices load while the views are staged.
   const uint4 xf_first = ld_stream4u(sc.soa + 6 * (size_t)sc.cap + tile_first * kTileObjects + (uint32_t)lane * kObjPerThread);
 
@@ -512,6 +512,7 @@ __global__ void move_object_kernel(float* soa, uint32_t cap, uint32_t from, uint
 
 int launch_cull(const CullLaunch& a, int grid, int vpp, void* stream)
 {
+  if (a.item_tiles < 1 || a.item_tiles > (uint32_t)kItemTiles) return -1;
   cudaStream_t s = static_cast<cudaStream_t>(stream);
   switch (vpp) {
     case 1: return launch_vpp<1>(a, grid, s);

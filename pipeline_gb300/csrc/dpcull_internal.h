@@ -36,10 +36,21 @@ constexpr int kItemTiles = 4;                      // tiles per work item (one w
 constexpr int kQueueCap = 1024;                    // undecided pairs a warp holds before a drain
 constexpr uint32_t kDeltaChunk = 4096;             // delta words per changed-list chunk
 
-// Work items of a scene: groups of kItemTiles tiles x view groups.
-DPCULL_HD_CONST uint32_t items_of(uint32_t n_tiles, uint32_t n_vgroups)
+// Work items of a scene: groups of item_tiles (1..kItemTiles) tiles x view groups.
+DPCULL_HD_CONST uint32_t items_of(uint32_t n_tiles, uint32_t n_vgroups, uint32_t item_tiles)
 {
-  return (n_tiles + kItemTiles - 1) / kItemTiles * n_vgroups;
+  return (n_tiles + item_tiles - 1) / item_tiles * n_vgroups;
+}
+
+// Tiles per work item for a launch of `tile_groups` (tiles x view groups) on `sm_count`
+// SMs: long items amortise each warp's exact drain, short ones keep every warp busy when
+// the launch is small.
+inline uint32_t item_tiles_for(uint64_t tile_groups, int sm_count)
+{
+  const uint64_t warps = (uint64_t)(sm_count > 0 ? sm_count : 1) * 24;
+  if (tile_groups >= warps * 8) return kItemTiles;
+  if (tile_groups >= warps * 4) return 2;
+  return 1;
 }
 constexpr int kMaxViewsPerPass = 8;                // views evaluated per object load
 constexpr uint32_t kMaxObjects = (1u << 30) - 1;   // keeps every index and count in 32 bits
@@ -60,7 +71,7 @@ struct CullScene {
   uint32_t n_views;
   uint32_t n_vgroups;      // ceil(n_views / views per pass)
   uint32_t n_tiles;
-  uint32_t item_begin;     // first work item of this scene (items_of(n_tiles, n_vgroups))
+  uint32_t item_begin;     // first work item of this scene (items_of(n_tiles, n_vgroups, ...))
 };
 
 struct alignas(16) CullView {   // 128 bytes; staged whole into shared memory by the cull
@@ -93,6 +104,7 @@ struct CullLaunch {
   uint32_t n_scenes;
   uint32_t n_items;
   uint32_t items_per_ticket; // items a warp claims per ticket (the "tiles per ticket" knob)
+  uint32_t item_tiles;       // tiles per work item, 1..kItemTiles
   uint32_t exact_only;       // 1 = skip the conservative prefilter (every pair exact)
   CullControl* ctl;
   CullScene one_scene;

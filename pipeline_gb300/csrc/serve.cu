@@ -357,6 +357,10 @@ bool launch(dpcull_server s, Slot& slot)
   cudaMemsetAsync(counts, 0, n_views * 4, slot.stream);
 
   const int vpp = vpp_for(max_views);
+  uint64_t tile_groups = 0;
+  for (auto& q : take)
+    tile_groups += (s->scenes[q.scene].cap / kTileObjects) * (uint64_t)((q.n_views + vpp - 1) / vpp);
+  const uint32_t item_tiles = item_tiles_for(tile_groups, s->sm_count);
   uint32_t items = 0, max_tiles = 1, vi = 0;
   size_t kept_words = 0;
   slot.bits_off.clear();
@@ -380,7 +384,7 @@ bool launch(dpcull_server s, Slot& slot)
     cs.n_vgroups = (q.n_views + vpp - 1) / vpp;
     cs.n_tiles = (uint32_t)(sc.cap / kTileObjects);
     cs.item_begin = items;
-    items += items_of(cs.n_tiles, cs.n_vgroups);
+    items += items_of(cs.n_tiles, cs.n_vgroups, item_tiles);
     max_tiles = std::max(max_tiles, cs.n_tiles);
     slot.h_scenes[i] = cs;
     slot.bits_off.push_back(words_off);
@@ -406,6 +410,7 @@ bool launch(dpcull_server s, Slot& slot)
   a.views = slot.d_views;
   a.n_scenes = (uint32_t)take.size();
   a.n_items = items;
+  a.item_tiles = item_tiles;
   a.items_per_ticket = 1;
   a.ctl = slot.ctl;
   const int occ = cull_max_ctas_per_sm(vpp);
