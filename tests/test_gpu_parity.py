@@ -417,3 +417,43 @@ def test_kernel_launch_counter(ctx):
     ctx.synchronize()
     assert ctx.kernel_launches > before
     ctx.group_destroy(g)
+
+
+def test_plan_read_empty_group_and_capacity(ctx):
+    """dpcull_plan_read over a plan whose jobs include an empty group: results come back in
+    job and view order (the empty group's list is empty), and a changed-list buffer that is
+    too small is reported as DPCULL_ERR_CAPACITY."""
+    from pipeline_gb300 import native
+
+    sc = W.stress_scene(seed=21, n_objects=50_000, n_transforms=2000)
+    g = setup_group(ctx, sc["lower"], sc["upper"], sc["xform"], sc["mats"])
+    empty = ctx.group_create()
+    ctx.group_set_objects(empty, np.zeros((3, 0), np.float32), np.zeros((3, 0), np.float32),
+                          np.zeros(0, np.uint32))
+    ctx.group_set_matrices(empty, sc["mats"])
+    r0 = [ctx.result_create(empty)]
+    rs = [ctx.result_create(g) for _ in range(3)]
+    vps = sc["vps"][:3]
+    p = ctx.plan_create([(empty, r0, vps[:1]), (g, rs, vps)], dict(views_per_pass=4, tiles_per_ticket=1, ctas_per_sm=0))
+    ctx.plan_launch(p)
+    n = 50_000
+    bits = [None] + [np.zeros((n + 31) // 32, np.uint32) for _ in range(3)]
+    changed = [None] + [np.zeros(n, np.uint32) for _ in range(3)]
+    n_ch = ctx.plan_read(p, bits, changed)
+    obbs = oracle.build_obbs(sc["lower"], sc["extent"], sc["xform"], sc["mats"])
+    all_ones = np.full((n + 31) // 32, 0xFFFFFFFF, np.uint32)  # a first cull: all visible
+    all_ones[-1] = (1 << (n % 32)) - 1 if n % 32 else 0xFFFFFFFF  # objects 0..n-1 only
+    assert n_ch[0] == 0
+    for v in range(3):
+        want = oracle.cull_obbs(obbs, vps[v], threads=8)
+        ch = oracle.update_changed(all_ones.copy(), want, n)
+        assert np.array_equal(bits[v + 1], want)
+        assert n_ch[v + 1] == len(ch) and np.array_equal(changed[v + 1][: len(ch)], ch)
+    # a buffer too small for a changed list
+    small = [None] + [np.zeros(1, np.uint32) for _ in range(3)]
+    if int(n_ch[1:].max()) > 1:
+        with pytest.raises(native.DpcullError):
+            ctx.plan_read(p, [None] * 4, small)
+    ctx.plan_destroy(p)
+    ctx.group_destroy(g)
+    ctx.group_destroy(empty)
