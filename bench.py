@@ -413,8 +413,14 @@ def run_hierarchy_config(ctx, args) -> dict:
     ctx.group_set_objects(g, sc["lower"], sc["extent"], sc["xform"])
     ctx.group_bind_device_matrices(g, dev, count)
     r = ctx.result_create(g)
-    idx = np.arange(1, used, dtype=np.uint32)
-    locs = np.ascontiguousarray(sc["locals"][1:])
+    # the per-frame inputs live in page-locked host memory, as an animation system's
+    # output buffers would: each upload is then one DMA (no host staging copy)
+    import torch
+
+    idx = torch.empty(used - 1, dtype=torch.int32, pin_memory=True).numpy().view(np.uint32)
+    idx[:] = np.arange(1, used, dtype=np.uint32)
+    locs = torch.empty(sc["locals"][1:].shape, dtype=torch.float32, pin_memory=True).numpy()
+    locs[:] = sc["locals"][1:]
     stream = torch.cuda.ExternalStream(ctx.stream)
     frames = sc["vps"].shape[0]
     for i in range(args.warmup):
@@ -430,7 +436,7 @@ def run_hierarchy_config(ctx, args) -> dict:
         with torch.cuda.stream(stream):
             ev[0].record(stream)
             u0 = time.perf_counter()
-            ctx.tree_set_locals(t.handle, idx, locs)  # host staging + H2D + scatter (dirty bits)
+            ctx.tree_set_locals(t.handle, idx, locs)  # H2D from page-locked memory + scatter (dirty bits)
             up_ms += (time.perf_counter() - u0) * 1e3
             ev[1].record(stream)
             ctx.tree_compute(t.handle)
@@ -447,7 +453,7 @@ def run_hierarchy_config(ctx, args) -> dict:
             "propagate_ms": prop_ms / n, "cull_ms": cull_ms / n,
             "propagate_transforms_per_s": (used - 1) / (prop_ms / n / 1e3),
             "object_views_per_s_e2e": 4_000_000 / (wall_ms / 1e3),
-            "note": "per frame: all 64k local matrices updated from host memory (4 MB), GPU propagation, "
+            "note": "per frame: all 64k local matrices updated from page-locked host memory (4 MB), GPU propagation, "
                     "cull through the device world matrices, changed list read back"}
 
 

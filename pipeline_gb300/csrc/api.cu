@@ -389,6 +389,27 @@ int stage_upload(dpcull_ctx c, int n, const void* const* src, const size_t* byte
     c->stage_pending = false;
   }
   if (!c->stage_ev) CU(cudaEventCreateWithFlags(&c->stage_ev, cudaEventDisableTiming));
+  // Sources in page-locked memory go to the device directly (one DMA each, no host copy);
+  // the call returns once they have landed (after the context's earlier work), so the
+  // caller may reuse its buffers at once, as with the staged path.
+  bool pinned = true;
+  for (int i = 0; i < n && pinned; ++i) {
+    cudaPointerAttributes at{};
+    if (cudaPointerGetAttributes(&at, src[i]) != cudaSuccess || at.type != cudaMemoryTypeHost) {
+      cudaGetLastError();
+      pinned = false;
+    }
+  }
+  if (pinned) {
+    for (int i = 0; i < n; ++i) {
+      dev[i] = c->stage_d + off[i];
+      CU(cudaMemcpyAsync(dev[i], src[i], bytes[i], cudaMemcpyHostToDevice, c->stream));
+    }
+    CU(cudaEventRecord(c->stage_ev, c->stream));
+    CU(cudaEventSynchronize(c->stage_ev));
+    c->stage_pending = false;
+    return DPCULL_OK;
+  }
   if (c->stage_pending) CU(cudaEventSynchronize(c->stage_ev));
   for (int i = 0; i < n; ++i) {
     memcpy(c->stage_h + off[i], src[i], bytes[i]);
