@@ -1332,7 +1332,7 @@ int dpcull_plan_launch(dpcull_ctx c, dpcull_plan ph)
   CU(cudaEventRecord(p->done[s], c->stream));
   p->pending[s] = true;
   p->next ^= 1;
-  c->launches++;
+  c->launches += 3;  // the graph's kernels: cull, chunk counts, changed-list emission
   return DPCULL_OK;
 }
 
