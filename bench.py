@@ -252,7 +252,12 @@ def run_ours(args, dist: Dist) -> dict | None:
     # -- serving loop (device-resident catalogue, continuous batching) --
     serving_res = None
     if args.serve_seconds > 0 and dist.rank == 0:
-        ctx.group_destroy(wl.g)  # free the stress scene before filling the budget
+        # free the stress scene, its plan and results before filling the budget
+        ctx.plan_destroy(wl.plan)
+        for r in wl.rs + wl.rp:
+            ctx.result_destroy(r)
+        ctx.group_destroy(wl.g)
+        torch.cuda.empty_cache()
         serving_res = run_serving(ctx, args)
 
     bytes_launch = wl.algorithmic_bytes(sum(changed))
@@ -318,13 +323,18 @@ def run_e2e(ctx, wl, frames, args, dist) -> dict:
         vps_pinned[:] = frames[i % len(frames)]
         ctx.plan_set_views(wl.plan, vps_pinned)
         ctx.plan_launch(wl.plan)
-        n_ch = ctx.plan_read(wl.plan, bits, changed)
+        if i:
+            ctx.plan_read_wait(wl.plan)  # the previous step's results are on the host
+        # this step's results: snapshot on the device, copies overlap the next step's cull
+        n_ch = ctx.plan_read_async(wl.plan, bits, changed)
         d2h += wl.v * (words * 4 + 4) + 4 * int(n_ch.sum())
+    ctx.plan_read_wait(wl.plan)
     dt = dist.max(time.perf_counter() - t0)
     return {"value": wl.object_views() * dist.world * steps / dt, "unit": "object-views/s",
             "ms_per_step": dt * 1e3 / steps, "h2d_bytes_per_step": wl.v * 64,
             "d2h_bytes_per_step": int(d2h / steps), "steps": steps,
-            "path": "plan_set_views + plan_launch + plan_read (every view's words and changed list; C ABI)"}
+            "path": "plan_set_views + plan_launch + plan_read_async / plan_read_wait (every view's words "
+                    "and changed list, copied while the next step culls; C ABI)"}
 
 
 def traffic_from_profile(wl) -> int | None:
@@ -532,7 +542,8 @@ def run_serving(ctx, args) -> dict:
                 "uploads": st["scene_uploads"], "upload_gb": st["upload_bytes"] / 1e9,
                 "batches": st["batches"], "max_batch_requests": st["max_batch_requests"],
                 "streams": 3, "scheduler": {k: st[k] for k in ("max_turn_us", "slow_turns",
-                                                               "max_upload_call_us", "max_evict_call_us")}})
+                                                               "max_upload_call_us", "max_evict_call_us",
+                                                               "reserved_bytes")}})
     return res
 
 

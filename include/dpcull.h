@@ -181,6 +181,16 @@ int dpcull_plan_kernel_ms(dpcull_ctx ctx, dpcull_plan p, uint32_t back, float* m
  * instead of one or two per result.  DPCULL_ERR_CAPACITY when a list does not fit. */
 int dpcull_plan_read(dpcull_ctx ctx, dpcull_plan p, uint32_t* const* bits, uint32_t* const* changed,
                      const size_t* changed_cap, size_t* n_changed);
+/* The same read without waiting for the copies: the results of the plan's last launch are
+ * snapshotted on the device, the call returns once their changed counts are known (after
+ * that launch's kernels) with n_changed filled in, and the copies to bits / changed land
+ * on a copy stream while the next dpcull_plan_launch runs.  The host buffers must stay
+ * valid and untouched until dpcull_plan_read_wait returns (the next read_async waits for
+ * the previous one's copies on the device).  No counterpart in the reference (it reads
+ * results synchronously). */
+int dpcull_plan_read_async(dpcull_ctx ctx, dpcull_plan p, uint32_t* const* bits,
+                           uint32_t* const* changed, const size_t* changed_cap, size_t* n_changed);
+int dpcull_plan_read_wait(dpcull_ctx ctx, dpcull_plan p);
 int dpcull_plan_destroy(dpcull_ctx ctx, dpcull_plan p);
 /* Autotunes views_per_pass / tiles_per_ticket / ctas_per_sm for the job list by timing
  * candidate launches (results of the jobs are overwritten). */
@@ -252,6 +262,7 @@ typedef struct dpcull_server_stats {
   uint64_t max_batch_requests, pending_requests;
   /* scheduler timing: longest turn, turns over 1 ms, longest upload / eviction call (us) */
   uint64_t max_turn_us, slow_turns, max_upload_call_us, max_evict_call_us;
+  uint64_t reserved_bytes;  /* budget mapped into the device pool at creation (0: grows on demand) */
 } dpcull_server_stats;
 
 /* Steady-clock seconds; the clock of dpcull_completion's timestamps. */

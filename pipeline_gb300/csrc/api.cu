@@ -126,6 +126,17 @@ struct Plan {
   std::vector<uint32_t> all_groups;    // every job's group (empty ones included)
   std::vector<uint32_t> all_results;   // every job's results, in job and view order
   uint32_t* h_counts = nullptr;        // pinned: changed counts read by dpcull_plan_read
+  // dpcull_plan_read_async: device snapshots of the results, copied out on copy_stream
+  cudaStream_t copy_stream = nullptr;
+  cudaEvent_t snap_ev = nullptr, counts_ev = nullptr, copies_ev = nullptr;
+  bool read_pending = false;
+  ResultCopy* d_copies = nullptr;      // one per result
+  uint32_t* snap = nullptr;            // words and changed lists of every result
+  uint32_t* d_counts = nullptr;        // changed counts, then the device error word pair
+  size_t snap_words = 0;
+  uint32_t snap_max_len = 0;
+  std::vector<size_t> snap_bits, snap_changed;  // offsets into snap
+  std::vector<size_t> snap_sizes;      // each result's size at set-up
   std::vector<uint64_t> all_incarnations;
   int next = 0;
   dpcull_tuning tuning{};
@@ -1384,6 +1395,114 @@ int dpcull_plan_read(dpcull_ctx c, dpcull_plan ph, uint32_t* const* bits, uint32
   return DPCULL_OK;
 }
 
+// Device snapshot storage and descriptors of a plan's results (set up on first use, and
+// again when a result's size changed).
+static int plan_snapshot_setup(dpcull_ctx c, Plan* p, const std::vector<Result*>& rs)
+{
+  const size_t nr = rs.size();
+  bool same = p->snap && p->snap_sizes.size() == nr;
+  for (size_t i = 0; same && i < nr; ++i) same = p->snap_sizes[i] == rs[i]->size_bits;
+  if (same) return DPCULL_OK;
+  if (p->read_pending) CU(cudaEventSynchronize(p->copies_ev));
+  p->read_pending = false;
+  CU(cudaStreamSynchronize(c->stream));
+  dfree(c, p->snap, p->snap_words * 4);
+  dfree(c, p->d_copies, p->snap_sizes.size() * sizeof(ResultCopy));
+  dfree(c, p->d_counts, (p->snap_sizes.size() + 2) * 4);
+  p->snap = nullptr;
+  p->d_copies = nullptr;
+  p->d_counts = nullptr;
+  p->snap_sizes.assign(nr, 0);
+  p->snap_bits.assign(nr, 0);
+  p->snap_changed.assign(nr, 0);
+  size_t total = 0;
+  uint32_t max_len = 1;
+  for (size_t i = 0; i < nr; ++i) {
+    const size_t n = rs[i]->size_bits, words = (n + 31) / 32;
+    p->snap_sizes[i] = n;
+    p->snap_bits[i] = total;
+    total += (words + 63) / 64 * 64;
+    p->snap_changed[i] = total;
+    total += (n + 63) / 64 * 64;
+    max_len = std::max<uint32_t>(max_len, (uint32_t)std::max(n, words));
+  }
+  p->snap_words = std::max<size_t>(total, 64);
+  p->snap_max_len = max_len;
+  int rc = dalloc(c, (void**)&p->snap, p->snap_words * 4);
+  if (!rc) rc = dalloc(c, (void**)&p->d_copies, std::max<size_t>(nr, 1) * sizeof(ResultCopy));
+  if (!rc) rc = dalloc(c, (void**)&p->d_counts, (nr + 2) * 4);
+  if (rc) return rc;
+  std::vector<ResultCopy> h(nr);
+  for (size_t i = 0; i < nr; ++i) {
+    h[i] = ResultCopy{rs[i]->bits, rs[i]->changed, rs[i]->n_changed, p->snap + p->snap_bits[i],
+                      p->snap + p->snap_changed[i], p->d_counts + i, (uint32_t)((rs[i]->size_bits + 31) / 32), 0};
+  }
+  if (nr) CU(cudaMemcpyAsync(p->d_copies, h.data(), nr * sizeof(ResultCopy), cudaMemcpyHostToDevice, c->stream));
+  if (!p->copy_stream) CU(cudaStreamCreateWithFlags(&p->copy_stream, cudaStreamNonBlocking));
+  if (!p->snap_ev) CU(cudaEventCreateWithFlags(&p->snap_ev, cudaEventDisableTiming));
+  if (!p->counts_ev) CU(cudaEventCreateWithFlags(&p->counts_ev, cudaEventDisableTiming));
+  if (!p->copies_ev) CU(cudaEventCreateWithFlags(&p->copies_ev, cudaEventDisableTiming));
+  return DPCULL_OK;
+}
+
+int dpcull_plan_read_async(dpcull_ctx c, dpcull_plan ph, uint32_t* const* bits, uint32_t* const* changed,
+                           const size_t* changed_cap, size_t* n_changed)
+{
+  Plan* p = get_plan(c, ph);
+  if (!p) return fail(DPCULL_ERR_INVALID_ARGUMENT, "bad plan %u", ph);
+  const size_t nr = p->all_results.size();
+  std::vector<Result*> rs(nr);
+  for (size_t i = 0; i < nr; ++i) {
+    rs[i] = get_result(c, p->all_results[i]);
+    if (!rs[i]) return fail(DPCULL_ERR_STATE, "plan %u: result %u was destroyed", ph, p->all_results[i]);
+  }
+  int rc = plan_snapshot_setup(c, p, rs);
+  if (rc) return rc;
+  // The snapshot overwrites what the previous read's copies are reading: wait for them
+  // on the device.
+  if (p->read_pending) CU(cudaStreamWaitEvent(c->stream, p->copies_ev, 0));
+  p->read_pending = false;
+  if (launch_snapshot(p->d_copies, (uint32_t)nr, p->snap_max_len, c->stream))
+    return cuda_fail(cudaGetLastError(), "snapshot launch");
+  c->launches++;
+  CU(cudaMemcpyAsync(p->d_counts + nr, &c->ctl->error, 2 * sizeof(unsigned int), cudaMemcpyDeviceToDevice,
+                     c->stream));
+  CU(cudaEventRecord(p->snap_ev, c->stream));
+  // The counts (and the error word) first: the list copies need their lengths.
+  CU(cudaStreamWaitEvent(p->copy_stream, p->snap_ev, 0));
+  CU(cudaMemcpyAsync(p->h_counts, p->d_counts, (nr + 2) * 4, cudaMemcpyDeviceToHost, p->copy_stream));
+  CU(cudaEventRecord(p->counts_ev, p->copy_stream));
+  CU(cudaEventSynchronize(p->counts_ev));
+  if (p->h_counts[nr]) return check_device_errors(c);
+  for (size_t i = 0; i < nr; ++i) {
+    const uint32_t cnt = p->h_counts[i];
+    if (n_changed) n_changed[i] = cnt;
+    if (changed && changed[i] && cnt && (!changed_cap || cnt > changed_cap[i]))
+      return fail(DPCULL_ERR_CAPACITY, "plan %u: result %zu has %u changed objects", ph, i, cnt);
+  }
+  for (size_t i = 0; i < nr; ++i) {
+    const uint32_t cnt = p->h_counts[i];
+    if (bits && bits[i] && p->snap_sizes[i])
+      CU(cudaMemcpyAsync(bits[i], p->snap + p->snap_bits[i], (p->snap_sizes[i] + 31) / 32 * 4,
+                         cudaMemcpyDeviceToHost, p->copy_stream));
+    if (changed && changed[i] && cnt)
+      CU(cudaMemcpyAsync(changed[i], p->snap + p->snap_changed[i], (size_t)cnt * 4, cudaMemcpyDeviceToHost,
+                         p->copy_stream));
+  }
+  CU(cudaEventRecord(p->copies_ev, p->copy_stream));
+  p->read_pending = true;
+  return DPCULL_OK;
+}
+
+int dpcull_plan_read_wait(dpcull_ctx c, dpcull_plan ph)
+{
+  Plan* p = get_plan(c, ph);
+  if (!p) return fail(DPCULL_ERR_INVALID_ARGUMENT, "bad plan %u", ph);
+  if (p->read_pending) CU(cudaEventSynchronize(p->copies_ev));
+  p->read_pending = false;
+  return DPCULL_OK;
+}
+
 int dpcull_plan_tuning(dpcull_ctx c, dpcull_plan ph, dpcull_tuning* out)
 {
   Plan* p = get_plan(c, ph);
@@ -1405,6 +1524,16 @@ int dpcull_plan_destroy(dpcull_ctx c, dpcull_plan ph)
     if (p->h_views[s]) cudaFreeHost(p->h_views[s]);
   }
   if (p->h_counts) cudaFreeHost(p->h_counts);
+  if (p->copy_stream) {
+    cudaStreamSynchronize(p->copy_stream);
+    cudaStreamDestroy(p->copy_stream);
+  }
+  if (p->snap_ev) cudaEventDestroy(p->snap_ev);
+  if (p->counts_ev) cudaEventDestroy(p->counts_ev);
+  if (p->copies_ev) cudaEventDestroy(p->copies_ev);
+  dfree(c, p->snap, p->snap_words * 4);
+  dfree(c, p->d_copies, std::max<size_t>(p->snap_sizes.size(), 1) * sizeof(ResultCopy));
+  dfree(c, p->d_counts, (p->snap_sizes.size() + 2) * 4);
   dfree(c, p->d_scenes, p->scenes.size() * sizeof(CullScene));
   dfree(c, p->d_views, p->views.size() * sizeof(CullView));
   *p = Plan();

@@ -501,6 +501,20 @@ __global__ void move_bit_kernel(uint32_t* bits, uint32_t size_bits, uint32_t old
   bits[new_index >> 5] = b ? (bits[new_index >> 5] | m) : (bits[new_index >> 5] & ~m);
 }
 
+// grid = (blocks, results): copies each result's words and changed list (its length read
+// here, on the device) into the snapshot buffers.
+__global__ void snapshot_kernel(const ResultCopy* copies)
+{
+  const ResultCopy c = copies[blockIdx.y];
+  const uint32_t count = *c.n_changed;
+  if (blockIdx.x == 0 && threadIdx.x == 0) *c.dst_count = count;
+  const uint32_t stride = gridDim.x * blockDim.x;
+  for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < c.n_words; i += stride)
+    c.dst_bits[i] = __ldcg(c.bits + i);
+  for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < count; i += stride)
+    c.dst_changed[i] = __ldcg(c.changed + i);
+}
+
 // GroupBitSet::removeObject moves the last object into the hole: SoA row copy.
 __global__ void move_object_kernel(float* soa, uint32_t cap, uint32_t from, uint32_t to)
 {
@@ -550,6 +564,14 @@ int launch_move_bit(uint32_t* bits, uint32_t size_bits, uint32_t old_index, uint
 {
   move_bit_kernel<<<1, 1, 0, static_cast<cudaStream_t>(stream)>>>(bits, size_bits, old_index,
                                                                   new_index);
+  return cudaGetLastError() == cudaSuccess ? 0 : -1;
+}
+
+int launch_snapshot(const ResultCopy* copies, uint32_t n, uint32_t max_len, void* stream)
+{
+  if (!n) return 0;
+  const uint32_t blocks = std::max<uint32_t>(1, std::min<uint32_t>(256, (max_len + 4095) / 4096));
+  snapshot_kernel<<<dim3(blocks, n), 256, 0, static_cast<cudaStream_t>(stream)>>>(copies);
   return cudaGetLastError() == cudaSuccess ? 0 : -1;
 }
 

@@ -154,4 +154,19 @@ int launch_move_bit(uint32_t* bits, uint32_t size_bits, uint32_t old_index, uint
                     void* stream);
 int launch_move_object(float* soa, uint32_t cap, uint32_t from, uint32_t to, void* stream);
 
+// Snapshot of a result for an asynchronous read: its visibility words, its changed list
+// (length read on the device) and that length.
+struct ResultCopy {
+  const uint32_t* bits;
+  const uint32_t* changed;
+  const uint32_t* n_changed;
+  uint32_t* dst_bits;
+  uint32_t* dst_changed;
+  uint32_t* dst_count;
+  uint32_t n_words;
+  uint32_t pad;
+};
+// One launch over `n` results (device array `copies`).
+int launch_snapshot(const ResultCopy* copies, uint32_t n, uint32_t max_len, void* stream);
+
 }  // namespace dpcull

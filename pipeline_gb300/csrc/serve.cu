@@ -515,6 +515,7 @@ int dpcull_server_create(dpcull_ctx ctx, uint64_t budget_bytes, uint32_t n_strea
     if (cudaMallocAsync(&reserve, budget_bytes, 0) == cudaSuccess) {
       cudaFreeAsync(reserve, 0);
       cudaStreamSynchronize(0);
+      s->stats.reserved_bytes = budget_bytes;
     }
     cudaGetLastError();
   }

@@ -84,6 +84,8 @@ _SIGS = {
     "dpcull_plan_tuning": (_I, [_P, _U32, C.POINTER(Tuning)]),
     "dpcull_plan_kernel_ms": (_I, [_P, _U32, _U32, C.POINTER(C.c_float)]),
     "dpcull_plan_read": (_I, [_P, _U32, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
+    "dpcull_plan_read_async": (_I, [_P, _U32, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
+    "dpcull_plan_read_wait": (_I, [_P, _U32]),
     "dpcull_plan_destroy": (_I, [_P, _U32]),
     "dpcull_autotune": (_I, [_P, C.POINTER(Job), _SZ, C.POINTER(Tuning)]),
     "dpcull_tree_create": (_I, [_P, _SZ, _UP]),
@@ -124,7 +126,8 @@ class ServerStats(C.Structure):
     _fields_ = [(name, C.c_uint64) for name in (
         "requests_submitted", "requests_completed", "batches", "scene_uploads", "scene_evictions",
         "upload_bytes", "resident_bytes", "resident_scenes", "budget_bytes", "max_batch_requests",
-        "pending_requests", "max_turn_us", "slow_turns", "max_upload_call_us", "max_evict_call_us")]
+        "pending_requests", "max_turn_us", "slow_turns", "max_upload_call_us", "max_evict_call_us",
+        "reserved_bytes")]
 
     def as_dict(self) -> dict:
         return {name: int(getattr(self, name)) for name, _ in self._fields_}
@@ -372,6 +375,20 @@ class Context:
         out = np.zeros(n, np.uint64)
         _check(self.lib.dpcull_plan_read(self.h, p, bp, cp, caps, out.ctypes.data))
         return out
+
+    def plan_read_async(self, p: int, bits: list, changed: list) -> np.ndarray:
+        """Starts reading every result of the plan's last launch into the given arrays (kept
+        alive and untouched until plan_read_wait); returns the changed-list lengths."""
+        n = len(bits)
+        bp = (C.c_void_p * n)(*[(b.ctypes.data if b is not None else None) for b in bits])
+        cp = (C.c_void_p * n)(*[(c.ctypes.data if c is not None else None) for c in changed])
+        caps = (C.c_size_t * n)(*[(c.size if c is not None else 0) for c in changed])
+        out = np.zeros(n, np.uint64)
+        _check(self.lib.dpcull_plan_read_async(self.h, p, bp, cp, caps, out.ctypes.data))
+        return out
+
+    def plan_read_wait(self, p: int) -> None:
+        _check(self.lib.dpcull_plan_read_wait(self.h, p))
 
     def plan_tuning(self, p: int) -> dict:
         t = Tuning()

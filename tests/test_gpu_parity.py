@@ -449,6 +449,18 @@ def test_plan_read_empty_group_and_capacity(ctx):
         ch = oracle.update_changed(all_ones.copy(), want, n)
         assert np.array_equal(bits[v + 1], want)
         assert n_ch[v + 1] == len(ch) and np.array_equal(changed[v + 1][: len(ch)], ch)
+    # the same through the asynchronous read, overlapped with the next launch
+    abits = [None] + [np.zeros((n + 31) // 32, np.uint32) for _ in range(3)]
+    achanged = [None] + [np.zeros(n, np.uint32) for _ in range(3)]
+    a_ch = ctx.plan_read_async(p, abits, achanged)
+    prev = [b.copy() for b in bits[1:]]
+    ctx.plan_set_views(p, np.stack([W.jitter_view(np.random.default_rng(5), v) for v in vps]))
+    ctx.plan_launch(p)  # runs while the copies land; must not disturb them
+    ctx.plan_read_wait(p)
+    assert np.array_equal(a_ch, n_ch)
+    for v in range(3):
+        assert np.array_equal(abits[v + 1], prev[v])
+        assert np.array_equal(achanged[v + 1][: n_ch[v + 1]], changed[v + 1][: n_ch[v + 1]])
     # a buffer too small for a changed list
     small = [None] + [np.zeros(1, np.uint32) for _ in range(3)]
     if int(n_ch[1:].max()) > 1:
