@@ -2,18 +2,20 @@
 //
 // One kernel serves the plain per-call path (one group, one view) and the batched
 // persistent path (many groups x many views).  Every warp works on its own: it pulls work
-// items from an atomic ticket, and a work item is up to 4 tiles of 128 objects (one
-// float4 of each SoA row per lane) of one scene with one group of up to VPP views:
+// items from an atomic ticket, and a work item is 1-4 tiles of 128 objects (one float4 of
+// each SoA row per lane; the launch picks the tiles per item) of one scene with one group
+// of up to VPP views:
 //   1. stage the views (view-projection matrices, output pointers) and their prefilter
 //      planes in the warp's shared memory, unless the previous item had the same views;
-//   2. per tile: 128-bit streaming loads of the SoA rows; per object, gather its world
-//      matrix (4 x 128-bit __ldg) and build its prefilter box; per view, the
+//   2. per tile: 128-bit streaming loads of the SoA rows (the transform-index row one tile
+//      ahead, so the matrix gathers go out with the other rows); per object, gather its
+//      world matrix (4 x 128-bit __ldg) and build its prefilter box; per view, the
 //      conservative prefilter (dpcull_prefilter.h) decides visible / invisible wherever
 //      the reference's rounded result is certain; the decided-visible words go to shared
 //      memory and the undecided (object, view) pairs to the warp's queue;
 //   3. all lanes run the queued pairs through the exact reference test (dpcull_exact.cuh)
 //      and set the visible ones in the words;
-//   4. per tile and view: XOR with the result's previous words (ResultBitSet::
+//   4. per view of the item: XOR with the result's previous words (ResultBitSet::
 //      updateChanged), store the new words where they changed and the delta words.
 // No warp waits for another.  Two small kernels then turn the delta words into the packed
 // ascending changed list (launch_changed_lists).
