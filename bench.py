@@ -284,7 +284,8 @@ def run_ours(args, dist: Dist) -> dict | None:
                      "peak_source": pk["source"], "algorithmic_bytes_per_launch": bytes_launch,
                      "kernel_ms": k_ms, "step_ms": ms_step,
                      "kernel": "cull_kernel: CUDA events recorded inside the plan graph right before "
-                               "and after the kernel, every timed step"},
+                               "and after the kernel, every timed step",
+                     "issue": issue_roofline(wl, k_ms, (clk or {}).get("sm_mhz"))},
         "e2e": e2e, "gpu_launches": launches, "clocks": clk, "parity_sample": parity,
         "changed_per_step": changed, "serving": serving_res,
     }
@@ -337,14 +338,42 @@ def run_e2e(ctx, wl, frames, args, dist) -> dict:
                     "and changed list, copied while the next step culls; C ABI)"}
 
 
-def traffic_from_profile(wl) -> int | None:
-    """DRAM bytes per launch from the committed ncu summary, scaled to this workload."""
+def _profile_scaled(wl, key: str) -> int | None:
+    """A per-launch count from the committed ncu summary of the stress kernel, scaled to this
+    workload by object-views."""
     p = ROOT / "profiles" / "cull_stress_traffic.json"
     if not p.exists():
         return None
     d = json.loads(p.read_text())
+    if key not in d:
+        return None
     scale = (wl.n * wl.v) / (d["objects"] * d["views"])
-    return int(d["dram_bytes_per_launch"] * scale)
+    return int(d[key] * scale)
+
+
+def traffic_from_profile(wl) -> int | None:
+    """DRAM bytes per launch from the committed ncu summary, scaled to this workload."""
+    return _profile_scaled(wl, "dram_bytes_per_launch")
+
+
+def issue_roofline(wl, k_ms: float, sm_mhz) -> dict | None:
+    """The second bound of the cull kernel: warp-instruction issue.  The instruction count
+    per launch comes from the committed ncu capture (scaled by object-views), the duration
+    from this run's in-graph events; the peak is one warp-instruction per scheduler (4 per
+    SM) per cycle at the median SM clock sampled during the timed region."""
+    import torch
+
+    inst = _profile_scaled(wl, "warp_instructions_per_launch")
+    if inst is None or not sm_mhz:
+        return None
+    sms = torch.cuda.get_device_properties(torch.cuda.current_device()).multi_processor_count
+    achieved = inst / (k_ms / 1e3) / 1e9
+    peak = sms * 4 * float(sm_mhz) * 1e6 / 1e9
+    return {"bound": "issue", "achieved": achieved, "peak": peak, "unit": "G warp-instructions/s",
+            "frac": achieved / peak, "warp_instructions_per_launch": inst,
+            "thread_instructions_per_object_view": inst * 32 / wl.object_views(),
+            "note": "instruction count from profiles/cull_stress_traffic.json scaled by object-views; "
+                    "peak = SMs x 4 schedulers x median sampled SM clock"}
 
 
 # ---- other configurations (separate JSON lines; not the headline) ------------------------------

@@ -77,7 +77,7 @@ extern "C" int dpcull_cull_noalloc(const float* objects, size_t cap, size_t n, c
     return noalloc_fail(DPCULL_ERR_INVALID_ARGUMENT, "dpcull_cull_noalloc: null pointer");
   if (cap % kTileObjects || cap < n || n_matrices > 0xFFFFFFFFull)
     return noalloc_fail(DPCULL_ERR_INVALID_ARGUMENT,
-                        "dpcull_cull_noalloc: cap must be a multiple of 1024 and at least n");
+                        "dpcull_cull_noalloc: cap must be a multiple of 128 and at least n");
   if (((uintptr_t)objects & 15) || ((uintptr_t)matrices & 15))
     return noalloc_fail(DPCULL_ERR_INVALID_ARGUMENT, "dpcull_cull_noalloc: objects and matrices must be 16-byte aligned");
   int device = 0;
