@@ -9,7 +9,8 @@
 //      planes in the warp's shared memory, unless the previous item had the same views;
 //   2. per tile: 128-bit streaming loads of the SoA rows (the transform-index row one tile
 //      ahead, so the matrix gathers go out with the other rows); per object, gather its
-//      world matrix (4 x 128-bit __ldg) and build its prefilter box; per view, the
+//      world matrix (2 x 256-bit loads, or 4 x 128-bit where the array is only 16-byte
+//      aligned) and build its prefilter box; per view, the
 //      conservative prefilter (dpcull_prefilter.h) decides visible / invisible wherever
 //      the reference's rounded result is certain; the decided-visible words go to shared
 //      memory and the undecided (object, view) pairs to the warp's queue;
@@ -73,6 +74,29 @@ __device__ __forceinline__ uint32_t find_scene(const CullScene* scenes, uint32_t
     else hi = mid;
   }
   return lo;
+}
+
+// One 64-byte world matrix (4 rows).  When the matrix array is 32-byte aligned (every
+// array this library allocates; bound arrays need only 16) two 256-bit loads replace the
+// four 128-bit ones: a gather instruction touches 32 different lines whatever its width,
+// so halving the instructions halves the gather's L1 wavefronts.
+__device__ __forceinline__ void load_matrix(const float* M, bool wide, float4& r0, float4& r1,
+                                            float4& r2, float4& r3)
+{
+  if (wide) {
+    asm("ld.global.nc.v8.f32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
+        : "=f"(r0.x), "=f"(r0.y), "=f"(r0.z), "=f"(r0.w), "=f"(r1.x), "=f"(r1.y), "=f"(r1.z), "=f"(r1.w)
+        : "l"(M));
+    asm("ld.global.nc.v8.f32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
+        : "=f"(r2.x), "=f"(r2.y), "=f"(r2.z), "=f"(r2.w), "=f"(r3.x), "=f"(r3.y), "=f"(r3.z), "=f"(r3.w)
+        : "l"(M + 8));
+  } else {
+    const float4* M4 = reinterpret_cast<const float4*>(M);
+    r0 = __ldg(M4 + 0);
+    r1 = __ldg(M4 + 1);
+    r2 = __ldg(M4 + 2);
+    r3 = __ldg(M4 + 3);
+  }
 }
 
 // Exact visibility of one object of the scene (reference operation order), reloading its
@@ -177,10 +201,11 @@ __device__ __forceinline__ uint32_t classify_tile(const CullLaunch& a, WarpShare
 
   uint32_t amb = 0;
   if (PF) {
-    // Prefilter boxes of the 4 objects first (the 16 matrix gathers overlap), then each
+    // Prefilter boxes of the 4 objects first (their matrix gathers overlap), then each
     // view's planes are read once for all 4 objects.
     pf::Box bx[kObjPerThread];
     uint32_t valid = 0;
+    const bool wide = ((uintptr_t)sc.mats & 31u) == 0;
 #pragma unroll
     for (int k = 0; k < kObjPerThread; ++k) {
       const uint32_t mi = compu(xf, k);
@@ -188,13 +213,7 @@ __device__ __forceinline__ uint32_t classify_tile(const CullLaunch& a, WarpShare
       const bool use = exists & (mi < sc.n_mats);
       if (exists && !use && atomicOr(&a.ctl->error, kErrBadTransform) == 0) a.ctl->error_info = obj0 + k;
       float4 r0 = make_float4(0.f, 0.f, 0.f, 0.f), r1 = r0, r2 = r0, r3 = r0;
-      if (use) {
-        const float4* M = mats + 4 * (size_t)mi;
-        r0 = __ldg(M + 0);
-        r1 = __ldg(M + 1);
-        r2 = __ldg(M + 2);
-        r3 = __ldg(M + 3);
-      }
+      if (use) load_matrix(sc.mats + 16 * (size_t)mi, wide, r0, r1, r2, r3);
       const pf::F4 m0{r0.x, r0.y, r0.z, r0.w}, m1{r1.x, r1.y, r1.z, r1.w};
       const pf::F4 m2{r2.x, r2.y, r2.z, r2.w}, m3{r3.x, r3.y, r3.z, r3.w};
       bx[k] = pf::make_box(comp(lx, k), comp(ly, k), comp(lz, k), comp(ex, k), comp(ey, k),

@@ -262,6 +262,41 @@ def test_hierarchy_propagate_then_cull(ctx):
     ctx.group_destroy(g)
 
 
+@pytest.mark.parametrize("offset_floats", [0, 4, 8, 12])
+def test_bound_matrices_any_16_byte_alignment(ctx, offset_floats):
+    """Device-bound matrix arrays need only 16-byte alignment: the 32-byte aligned ones
+    (offsets 0 and 8 floats) take the 256-bit matrix loads, the others the 128-bit ones;
+    both are bit-exact against the oracle, in the plain and the batched launch."""
+    import torch
+
+    rng = np.random.default_rng(21)
+    n, n_mats = 70_001, 4096
+    lower, _, extent = W.random_boxes(rng, n)
+    mats = W.random_matrices(rng, n_mats)
+    xform = rng.integers(0, n_mats, n).astype(np.uint32)
+    buf = torch.zeros(n_mats * 16 + 16, dtype=torch.float32, device="cuda")
+    view = buf[offset_floats: offset_floats + n_mats * 16]
+    view.copy_(torch.from_numpy(np.ascontiguousarray(mats).reshape(-1)))
+    torch.cuda.synchronize()
+    assert view.data_ptr() % 32 == (0 if offset_floats % 8 == 0 else 16)
+    g = ctx.group_create()
+    ctx.group_set_objects(g, lower, extent, xform)
+    ctx.group_bind_device_matrices(g, view.data_ptr(), n_mats)
+    vps = W.cube_face_views()[:3] + W.stereo_views()
+    exp = port_frames(dict(lower=lower, extent=extent, xform=xform, mats=mats), vps)
+    r = ctx.result_create(g)
+    for vp, (bits, ch) in zip(vps, exp):
+        ctx.cull(g, r, vp)
+        assert np.array_equal(ctx.result_bits(r), bits)
+        assert np.array_equal(ctx.result_changed(r), ch)
+    rs = [ctx.result_create(g) for _ in vps]
+    ctx.cull_batched([(g, rs, vps)])
+    for rv, (bits, _) in zip(rs, exp):
+        assert np.array_equal(ctx.result_bits(rv), bits)
+    ctx.group_destroy(g)
+    del buf
+
+
 def test_stress_full_size_eight_views(ctx):
     """16M objects over 1M shared transforms, 8 views, one batched launch: every visibility
     word of every view equals the oracle's (multi-threaded port)."""
