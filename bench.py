@@ -316,26 +316,32 @@ def run_e2e(ctx, wl, frames, args, dist) -> dict:
     changed = [torch.empty(wl.n, dtype=torch.int32, pin_memory=True).numpy().view(np.uint32)
                for _ in range(wl.v)]
     vps_pinned = torch.empty((wl.v, 16), dtype=torch.float32, pin_memory=True).numpy()
-    steps = max(3, min(args.steps, 20))
+    steps = max(3, min(args.steps, 200))
     d2h = 0
     dist.barrier()
     t0 = time.perf_counter()
     for i in range(steps):
         vps_pinned[:] = frames[i % len(frames)]
         ctx.plan_set_views(wl.plan, vps_pinned)
+        if i:
+            ctx.plan_snapshot(wl.plan)  # step i-1's results, before step i overwrites them
         ctx.plan_launch(wl.plan)
         if i:
-            ctx.plan_read_wait(wl.plan)  # the previous step's results are on the host
-        # this step's results: snapshot on the device, copies overlap the next step's cull
-        n_ch = ctx.plan_read_async(wl.plan, bits, changed)
-        d2h += wl.v * (words * 4 + 4) + 4 * int(n_ch.sum())
+            ctx.plan_read_wait(wl.plan)  # step i-2's results are on the host
+            # step i-1's results: copies overlap step i's cull, which is already queued
+            n_ch = ctx.plan_read_async(wl.plan, bits, changed)
+            d2h += wl.v * (words * 4 + 4) + 4 * int(n_ch.sum())
+    ctx.plan_read_wait(wl.plan)
+    n_ch = ctx.plan_read_async(wl.plan, bits, changed)  # the last step's results
+    d2h += wl.v * (words * 4 + 4) + 4 * int(n_ch.sum())
     ctx.plan_read_wait(wl.plan)
     dt = dist.max(time.perf_counter() - t0)
     return {"value": wl.object_views() * dist.world * steps / dt, "unit": "object-views/s",
             "ms_per_step": dt * 1e3 / steps, "h2d_bytes_per_step": wl.v * 64,
             "d2h_bytes_per_step": int(d2h / steps), "steps": steps,
-            "path": "plan_set_views + plan_launch + plan_read_async / plan_read_wait (every view's words "
-                    "and changed list, copied while the next step culls; C ABI)"}
+            "path": "plan_set_views + plan_snapshot + plan_launch + plan_read_async / plan_read_wait "
+                    "(every view's words and changed list of the previous step, copied while this "
+                    "step culls; C ABI)"}
 
 
 def _profile_scaled(wl, key: str) -> int | None:

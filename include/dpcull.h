@@ -186,10 +186,17 @@ int dpcull_plan_read(dpcull_ctx ctx, dpcull_plan p, uint32_t* const* bits, uint3
  * that launch's kernels) with n_changed filled in, and the copies to bits / changed land
  * on a copy stream while the next dpcull_plan_launch runs.  The host buffers must stay
  * valid and untouched until dpcull_plan_read_wait returns (the next read_async waits for
- * the previous one's copies on the device).  No counterpart in the reference (it reads
- * results synchronously). */
+ * the previous one's copies on the device).  When dpcull_plan_snapshot was called since the
+ * last read, this reads that snapshot instead (results of the launch before the snapshot
+ * call), so a frame loop can launch the next frame before it waits:
+ *   set_views(i); snapshot (frame i-1); launch(i); read_wait; read_async (frame i-1).
+ * No counterpart in the reference (it reads results synchronously). */
 int dpcull_plan_read_async(dpcull_ctx ctx, dpcull_plan p, uint32_t* const* bits,
                            uint32_t* const* changed, const size_t* changed_cap, size_t* n_changed);
+/* Snapshots the results of the plan's last launch on the device and starts copying their
+ * changed counts to the host, without waiting; the next dpcull_plan_read_async reads this
+ * snapshot.  A later dpcull_plan_launch may overwrite the results themselves. */
+int dpcull_plan_snapshot(dpcull_ctx ctx, dpcull_plan p);
 int dpcull_plan_read_wait(dpcull_ctx ctx, dpcull_plan p);
 int dpcull_plan_destroy(dpcull_ctx ctx, dpcull_plan p);
 /* Autotunes views_per_pass / tiles_per_ticket / ctas_per_sm for the job list by timing

@@ -129,7 +129,8 @@ struct Plan {
   // dpcull_plan_read_async: device snapshots of the results, copied out on copy_stream
   cudaStream_t copy_stream = nullptr;
   cudaEvent_t snap_ev = nullptr, counts_ev = nullptr, copies_ev = nullptr;
-  bool read_pending = false;
+  bool read_pending = false;           // copies issued, not yet waited for
+  bool snap_pending = false;           // snapshot taken (dpcull_plan_snapshot), not yet read
   ResultCopy* d_copies = nullptr;      // one per result
   uint32_t* snap = nullptr;            // words and changed lists of every result
   uint32_t* d_counts = nullptr;        // changed counts, then the device error word pair
@@ -1405,6 +1406,7 @@ static int plan_snapshot_setup(dpcull_ctx c, Plan* p, const std::vector<Result*>
   if (same) return DPCULL_OK;
   if (p->read_pending) CU(cudaEventSynchronize(p->copies_ev));
   p->read_pending = false;
+  p->snap_pending = false;
   CU(cudaStreamSynchronize(c->stream));
   dfree(c, p->snap, p->snap_words * 4);
   dfree(c, p->d_copies, p->snap_sizes.size() * sizeof(ResultCopy));
@@ -1445,19 +1447,27 @@ static int plan_snapshot_setup(dpcull_ctx c, Plan* p, const std::vector<Result*>
   return DPCULL_OK;
 }
 
-int dpcull_plan_read_async(dpcull_ctx c, dpcull_plan ph, uint32_t* const* bits, uint32_t* const* changed,
-                           const size_t* changed_cap, size_t* n_changed)
+// The results of a plan's launches, in job and view order (every one still alive).
+static int plan_results(dpcull_ctx c, dpcull_plan ph, Plan* p, std::vector<Result*>& rs)
 {
-  Plan* p = get_plan(c, ph);
-  if (!p) return fail(DPCULL_ERR_INVALID_ARGUMENT, "bad plan %u", ph);
   const size_t nr = p->all_results.size();
-  std::vector<Result*> rs(nr);
+  rs.resize(nr);
   for (size_t i = 0; i < nr; ++i) {
     rs[i] = get_result(c, p->all_results[i]);
     if (!rs[i]) return fail(DPCULL_ERR_STATE, "plan %u: result %u was destroyed", ph, p->all_results[i]);
   }
-  int rc = plan_snapshot_setup(c, p, rs);
+  return DPCULL_OK;
+}
+
+int dpcull_plan_snapshot(dpcull_ctx c, dpcull_plan ph)
+{
+  Plan* p = get_plan(c, ph);
+  if (!p) return fail(DPCULL_ERR_INVALID_ARGUMENT, "bad plan %u", ph);
+  std::vector<Result*> rs;
+  int rc = plan_results(c, ph, p, rs);
+  if (!rc) rc = plan_snapshot_setup(c, p, rs);
   if (rc) return rc;
+  const size_t nr = rs.size();
   // The snapshot overwrites what the previous read's copies are reading: wait for them
   // on the device.
   if (p->read_pending) CU(cudaStreamWaitEvent(c->stream, p->copies_ev, 0));
@@ -1468,10 +1478,30 @@ int dpcull_plan_read_async(dpcull_ctx c, dpcull_plan ph, uint32_t* const* bits, 
   CU(cudaMemcpyAsync(p->d_counts + nr, &c->ctl->error, 2 * sizeof(unsigned int), cudaMemcpyDeviceToDevice,
                      c->stream));
   CU(cudaEventRecord(p->snap_ev, c->stream));
-  // The counts (and the error word) first: the list copies need their lengths.
+  // The counts (and the error word) go to the host first: the list copies need their
+  // lengths.
   CU(cudaStreamWaitEvent(p->copy_stream, p->snap_ev, 0));
   CU(cudaMemcpyAsync(p->h_counts, p->d_counts, (nr + 2) * 4, cudaMemcpyDeviceToHost, p->copy_stream));
   CU(cudaEventRecord(p->counts_ev, p->copy_stream));
+  p->snap_pending = true;
+  return DPCULL_OK;
+}
+
+int dpcull_plan_read_async(dpcull_ctx c, dpcull_plan ph, uint32_t* const* bits, uint32_t* const* changed,
+                           const size_t* changed_cap, size_t* n_changed)
+{
+  Plan* p = get_plan(c, ph);
+  if (!p) return fail(DPCULL_ERR_INVALID_ARGUMENT, "bad plan %u", ph);
+  std::vector<Result*> rs;
+  int rc = plan_results(c, ph, p, rs);
+  if (rc) return rc;
+  // Without a pending snapshot, take one of the last launch now.
+  if (!p->snap_pending) {
+    rc = dpcull_plan_snapshot(c, ph);
+    if (rc) return rc;
+  }
+  p->snap_pending = false;
+  const size_t nr = rs.size();
   CU(cudaEventSynchronize(p->counts_ev));
   if (p->h_counts[nr]) return check_device_errors(c);
   for (size_t i = 0; i < nr; ++i) {

@@ -86,6 +86,7 @@ _SIGS = {
     "dpcull_plan_read": (_I, [_P, _U32, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
     "dpcull_plan_read_async": (_I, [_P, _U32, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
     "dpcull_plan_read_wait": (_I, [_P, _U32]),
+    "dpcull_plan_snapshot": (_I, [_P, _U32]),
     "dpcull_plan_destroy": (_I, [_P, _U32]),
     "dpcull_autotune": (_I, [_P, C.POINTER(Job), _SZ, C.POINTER(Tuning)]),
     "dpcull_tree_create": (_I, [_P, _SZ, _UP]),
@@ -389,6 +390,11 @@ class Context:
 
     def plan_read_wait(self, p: int) -> None:
         _check(self.lib.dpcull_plan_read_wait(self.h, p))
+
+    def plan_snapshot(self, p: int) -> None:
+        """Snapshots the results of the plan's last launch without waiting; the next
+        plan_read_async reads the snapshot (so the next launch can go out first)."""
+        _check(self.lib.dpcull_plan_snapshot(self.h, p))
 
     def plan_tuning(self, p: int) -> dict:
         t = Tuning()

@@ -215,6 +215,57 @@ def test_plan_graph_frames(ctx):
     ctx.group_destroy(g)
 
 
+def test_plan_snapshot_pipelined_frames(ctx):
+    """The pipelined frame loop: frame i-1 is snapshotted before frame i is launched and
+    read while frame i culls.  Every frame's words and changed lists reach the host
+    bit-exact, although the results on the device already hold the next frame."""
+    sc = W.stress_scene(seed=12, n_objects=250_001, n_transforms=10_000)
+    g = setup_group(ctx, sc["lower"], sc["upper"], sc["xform"], sc["mats"])
+    nv = 6
+    rs = [ctx.result_create(g) for _ in range(nv)]
+    p = ctx.plan_create([(g, rs, sc["vps"][:nv])], dict(views_per_pass=8, tiles_per_ticket=1, ctas_per_sm=0))
+    rng = np.random.default_rng(5)
+    frames = [sc["vps"][:nv]] + [np.stack([W.jitter_view(rng, v) for v in sc["vps"][:nv]]) for _ in range(5)]
+    obbs = oracle.build_obbs(sc["lower"], sc["extent"], sc["xform"], sc["mats"])
+    n = 250_001
+    expect = []
+    prev = [np.full((n + 31) // 32, 0xFFFFFFFF, np.uint32) for _ in range(nv)]
+    prev = [np.where(np.arange(len(w)) == len(w) - 1, (1 << (n % 32)) - 1, w).astype(np.uint32) for w in prev]
+    for vps in frames:
+        fr = []
+        for v in range(nv):
+            bits = oracle.cull_obbs(obbs, vps[v], threads=8)
+            fr.append((bits, oracle.update_changed(prev[v], bits, n)))
+        expect.append(fr)
+    out_bits = [np.zeros((n + 31) // 32, np.uint32) for _ in range(nv)]
+    out_changed = [np.zeros(n, np.uint32) for _ in range(nv)]
+
+    def check(k, n_ch):
+        for v in range(nv):
+            bits, ch = expect[k][v]
+            assert np.array_equal(out_bits[v], bits), (k, v)
+            assert n_ch[v] == len(ch) and np.array_equal(out_changed[v][: len(ch)], ch), (k, v)
+
+    for i, vps in enumerate(frames):
+        ctx.plan_set_views(p, vps)
+        if i:
+            ctx.plan_snapshot(p)
+        ctx.plan_launch(p)
+        if i:
+            ctx.plan_read_wait(p)
+            n_ch = ctx.plan_read_async(p, out_bits, out_changed)
+            ctx.plan_read_wait(p)
+            check(i - 1, n_ch)
+    n_ch = ctx.plan_read_async(p, out_bits, out_changed)  # no snapshot pending: the last launch
+    ctx.plan_read_wait(p)
+    check(len(frames) - 1, n_ch)
+    # the device results hold the last frame
+    for v in range(nv):
+        assert np.array_equal(ctx.result_bits(rs[v]), expect[-1][v][0])
+    ctx.plan_destroy(p)
+    ctx.group_destroy(g)
+
+
 def test_plan_autotuned(ctx, tmp_path, monkeypatch):
     sc = W.stress_scene(seed=10, n_objects=200_000, n_transforms=5000)
     g = setup_group(ctx, sc["lower"], sc["upper"], sc["xform"], sc["mats"])
