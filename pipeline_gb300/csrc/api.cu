@@ -444,6 +444,8 @@ int check_device_errors(dpcull_ctx c)
     CU(cudaStreamSynchronize(c->stream));
     if (err & kErrBadTransform)
       return fail(DPCULL_ERR_OUT_OF_RANGE, "object %u has a transform index past the matrix array", info);
+    if (err & kErrMisaligned)
+      return fail(DPCULL_ERR_STATE, "work item %u: a matrix array moved off its 32-byte alignment", info);
   }
   return DPCULL_OK;
 }
@@ -515,19 +517,26 @@ int persistent_grid(dpcull_ctx c, uint32_t vpp, uint32_t ctas_per_sm, uint32_t n
   return (int)std::max<long long>(grid, 1);
 }
 
+uint32_t max_words_of(const std::vector<CullScene>& scenes);
+
 // The cull over all scenes and views, then the changed-list assembly of every view.
-// k0 / k1 (optional, timing events) are recorded right before and after the cull kernel;
-// inside a stream capture they become event-record nodes visible outside the graph.
+// d_scenes is the device copy of `scenes`.  k0 / k1 (optional, timing events) are recorded
+// right before and after the cull kernel; inside a stream capture they become
+// event-record nodes visible outside the graph.
 int launch_batch(dpcull_ctx c, const CullScene* d_scenes, const CullView* d_views,
-                 uint32_t n_scenes, uint32_t n_views, uint32_t max_words, uint32_t n_items,
+                 const std::vector<CullScene>& scenes, uint32_t n_views, uint32_t n_items,
                  uint32_t item_tiles, const dpcull_tuning& t, cudaStream_t s,
                  cudaEvent_t k0 = nullptr, cudaEvent_t k1 = nullptr)
 {
   if (n_views > 65535) return fail(DPCULL_ERR_INVALID_ARGUMENT, "at most 65535 views per launch");
+  const uint32_t max_words = max_words_of(scenes);
   CullLaunch a{};
   a.scenes = d_scenes;
   a.views = d_views;
-  a.n_scenes = n_scenes;
+  a.n_scenes = (uint32_t)scenes.size();
+  a.wide_mats = 1;  // 256-bit matrix loads only if every scene's array allows them
+  for (const CullScene& sc : scenes)
+    if ((uintptr_t)sc.mats & 31u) a.wide_mats = 0;
   a.n_items = n_items;
   a.item_tiles = item_tiles;
   a.items_per_ticket = std::max<uint32_t>(1, t.tiles_per_ticket);
@@ -1118,8 +1127,7 @@ int dpcull_cull_batched(dpcull_ctx c, const dpcull_job* jobs, size_t n_jobs, con
   }
   cudaMemcpyAsync(ds, scenes.data(), scenes.size() * sizeof(CullScene), cudaMemcpyHostToDevice, c->stream);
   cudaMemcpyAsync(dv, views.data(), views.size() * sizeof(CullView), cudaMemcpyHostToDevice, c->stream);
-  rc = launch_batch(c, ds, dv, (uint32_t)scenes.size(), (uint32_t)views.size(), max_words_of(scenes),
-                    items, item_tiles, t, c->stream);
+  rc = launch_batch(c, ds, dv, scenes, (uint32_t)views.size(), items, item_tiles, t, c->stream);
   cudaStreamSynchronize(c->stream);
   dfree(c, ds, scenes.size() * sizeof(CullScene));
   dfree(c, dv, views.size() * sizeof(CullView));
@@ -1138,9 +1146,8 @@ static int plan_capture(dpcull_ctx c, Plan& p, int slot)
   int rc = DPCULL_OK;
   if (e == cudaSuccess) {
     const uint64_t before = c->launches;
-    rc = launch_batch(c, p.d_scenes, p.d_views, (uint32_t)p.scenes.size(), (uint32_t)p.views.size(),
-                      max_words_of(p.scenes), p.n_items, p.item_tiles, p.tuning, cs, p.kt[slot][0],
-                      p.kt[slot][1]);
+    rc = launch_batch(c, p.d_scenes, p.d_views, p.scenes, (uint32_t)p.views.size(), p.n_items,
+                      p.item_tiles, p.tuning, cs, p.kt[slot][0], p.kt[slot][1]);
     c->launches = before;  // counted when the graph is replayed
   }
   cudaError_t e2 = cudaStreamEndCapture(cs, &graph);
@@ -1160,10 +1167,10 @@ static int time_batch(dpcull_ctx c, const CullScene* ds, const CullView* dv,
   cudaEvent_t e0, e1;
   CU(cudaEventCreate(&e0));
   CU(cudaEventCreate(&e1));
-  const uint32_t ns = (uint32_t)sc.size(), nvw = (uint32_t)vw.size(), mt = max_words_of(sc);
-  int rc = launch_batch(c, ds, dv, ns, nvw, mt, items, item_tiles, t, c->stream);  // warm-up
+  const uint32_t nvw = (uint32_t)vw.size();
+  int rc = launch_batch(c, ds, dv, sc, nvw, items, item_tiles, t, c->stream);  // warm-up
   if (!rc) cudaEventRecord(e0, c->stream);
-  for (int i = 0; i < reps && !rc; ++i) rc = launch_batch(c, ds, dv, ns, nvw, mt, items, item_tiles, t, c->stream);
+  for (int i = 0; i < reps && !rc; ++i) rc = launch_batch(c, ds, dv, sc, nvw, items, item_tiles, t, c->stream);
   if (!rc) {
     cudaEventRecord(e1, c->stream);
     cudaEventSynchronize(e1);

@@ -177,8 +177,9 @@ __device__ __forceinline__ void drain_queue(WarpShared& ws, const CullScene& sc,
 }
 
 // Classification of one tile into the item's words (visible objects) and queue
-// (undecided pairs).  Returns the new queue length.
-template <int VPP, bool PF>
+// (undecided pairs).  Returns the new queue length.  WIDE: the scene's matrix array is
+// 32-byte aligned (two 256-bit loads per matrix).
+template <int VPP, bool PF, bool WIDE>
 __device__ __forceinline__ uint32_t classify_tile(const CullLaunch& a, WarpShared& ws, const CullScene& sc,
                                                   uint32_t tile, uint32_t t, uint32_t tile_first,
                                                   uint32_t n_t, int nv, uint32_t qn, int lane,
@@ -205,15 +206,14 @@ __device__ __forceinline__ uint32_t classify_tile(const CullLaunch& a, WarpShare
     // view's planes are read once for all 4 objects.
     pf::Box bx[kObjPerThread];
     uint32_t valid = 0;
-    const bool wide = ((uintptr_t)sc.mats & 31u) == 0;
-#pragma unroll
+  #pragma unroll
     for (int k = 0; k < kObjPerThread; ++k) {
       const uint32_t mi = compu(xf, k);
       const bool exists = obj0 + k < sc.n_objects;
       const bool use = exists & (mi < sc.n_mats);
       if (exists && !use && atomicOr(&a.ctl->error, kErrBadTransform) == 0) a.ctl->error_info = obj0 + k;
       float4 r0 = make_float4(0.f, 0.f, 0.f, 0.f), r1 = r0, r2 = r0, r3 = r0;
-      if (use) load_matrix(sc.mats + 16 * (size_t)mi, wide, r0, r1, r2, r3);
+      if (use) load_matrix(sc.mats + 16 * (size_t)mi, WIDE, r0, r1, r2, r3);
       const pf::F4 m0{r0.x, r0.y, r0.z, r0.w}, m1{r1.x, r1.y, r1.z, r1.w};
       const pf::F4 m2{r2.x, r2.y, r2.z, r2.w}, m3{r3.x, r3.y, r3.z, r3.w};
       bx[k] = pf::make_box(comp(lx, k), comp(ly, k), comp(lz, k), comp(ex, k), comp(ey, k),
@@ -309,7 +309,7 @@ __device__ __forceinline__ void finish_item(const WarpShared& ws, uint32_t tile_
 // One work item (up to kItemTiles tiles of 128 objects x one group of up to VPP views)
 // by one warp.  ws.sc and `vkey` cache the warp's current scene and staged view group
 // across items.
-template <int VPP, bool PF>
+template <int VPP, bool PF, bool WIDE>
 __device__ __forceinline__ void warp_item(const CullLaunch& a, uint32_t item, WarpShared& ws,
                                           uint32_t& vkey)
 {
@@ -323,6 +323,10 @@ __device__ __forceinline__ void warp_item(const CullLaunch& a, uint32_t item, Wa
     __syncwarp();
   }
   const CullScene& sc = ws.sc;
+  if (WIDE && ((uintptr_t)sc.mats & 31u)) {  // the launch's alignment promise does not hold:
+    if (lane == 0 && atomicOr(&a.ctl->error, kErrMisaligned) == 0) a.ctl->error_info = item;
+    return;                                  // report it, load nothing
+  }
   const uint32_t local = item - sc.item_begin;
   const uint32_t group = local / sc.n_vgroups;
   const uint32_t vfirst = (local - group * sc.n_vgroups) * VPP;
@@ -351,7 +355,7 @@ __device__ __forceinline__ void warp_item(const CullLaunch& a, uint32_t item, Wa
   uint4 xf = xf_first;
   for (uint32_t t = 0; t < n_t; ++t) {
     uint4 xf_next = make_uint4(0u, 0u, 0u, 0u);
-    qn = classify_tile<VPP, PF>(a, ws, sc, tile_first + t, t, tile_first, n_t, nv, qn, lane, xf, xf_next);
+    qn = classify_tile<VPP, PF, WIDE>(a, ws, sc, tile_first + t, t, tile_first, n_t, nv, qn, lane, xf, xf_next);
     xf = xf_next;
   }
   if (PF && qn) drain_queue(ws, sc, tile_first, qn, lane);
@@ -359,7 +363,7 @@ __device__ __forceinline__ void warp_item(const CullLaunch& a, uint32_t item, Wa
   finish_item<VPP>(ws, tile_first, n_t, nv, lane);
 }
 
-template <int VPP, bool PF>
+template <int VPP, bool PF, bool WIDE>
 __global__ void __launch_bounds__(kThreads, 3) cull_kernel(const __grid_constant__ CullLaunch a)
 {
   __shared__ WarpShared wsh[kThreads / 32];
@@ -381,7 +385,7 @@ __global__ void __launch_bounds__(kThreads, 3) cull_kernel(const __grid_constant
     uint32_t next = 0;
     if (lane == 0) next = atomicAdd(&ctl->ticket, a.items_per_ticket);
     const uint32_t last = min(first + a.items_per_ticket, a.n_items);
-    for (uint32_t item = first; item < last; ++item) warp_item<VPP, PF>(a, item, ws, vkey);
+    for (uint32_t item = first; item < last; ++item) warp_item<VPP, PF, WIDE>(a, item, ws, vkey);
     first = __shfl_sync(0xffffffffu, next, 0);
   }
   __syncthreads();
@@ -495,8 +499,9 @@ __global__ void __launch_bounds__(kScanThreads)
 template <int VPP>
 int launch_vpp(const CullLaunch& a, int grid, cudaStream_t s)
 {
-  if (a.exact_only) cull_kernel<VPP, false><<<grid, kThreads, 0, s>>>(a);
-  else cull_kernel<VPP, true><<<grid, kThreads, 0, s>>>(a);
+  if (a.exact_only) cull_kernel<VPP, false, false><<<grid, kThreads, 0, s>>>(a);
+  else if (a.wide_mats) cull_kernel<VPP, true, true><<<grid, kThreads, 0, s>>>(a);
+  else cull_kernel<VPP, true, false><<<grid, kThreads, 0, s>>>(a);
   return cudaGetLastError() == cudaSuccess ? 0 : -1;
 }
 
@@ -504,7 +509,7 @@ template <int VPP>
 int max_ctas()
 {
   int n = 0;
-  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, cull_kernel<VPP, true>, kThreads, 0) != cudaSuccess)
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, cull_kernel<VPP, true, true>, kThreads, 0) != cudaSuccess)
     return 1;
   return n > 0 ? n : 1;
 }
@@ -545,9 +550,11 @@ __global__ void move_object_kernel(float* soa, uint32_t cap, uint32_t from, uint
 
 }  // namespace
 
-int launch_cull(const CullLaunch& a, int grid, int vpp, void* stream)
+int launch_cull(const CullLaunch& args, int grid, int vpp, void* stream)
 {
-  if (a.item_tiles < 1 || a.item_tiles > (uint32_t)kItemTiles) return -1;
+  if (args.item_tiles < 1 || args.item_tiles > (uint32_t)kItemTiles) return -1;
+  CullLaunch a = args;
+  if (!a.scenes) a.wide_mats = ((uintptr_t)a.one_scene.mats & 31u) == 0 ? 1u : 0u;
   cudaStream_t s = static_cast<cudaStream_t>(stream);
   switch (vpp) {
     case 1: return launch_vpp<1>(a, grid, s);

@@ -60,6 +60,7 @@ DPCULL_HD_CONST size_t chunks_of(size_t n_words) { return (n_words + kDeltaChunk
 
 // Error bits reported through CullControl::error.
 constexpr uint32_t kErrBadTransform = 1u;   // transform index >= matrix count
+constexpr uint32_t kErrMisaligned = 2u;     // a wide launch met a matrix array not 32-byte aligned
 
 struct CullScene {
   const float* soa;        // base of the group's SoA block
@@ -106,6 +107,8 @@ struct CullLaunch {
   uint32_t items_per_ticket; // items a warp claims per ticket (the "tiles per ticket" knob)
   uint32_t item_tiles;       // tiles per work item, 1..kItemTiles
   uint32_t exact_only;       // 1 = skip the conservative prefilter (every pair exact)
+  uint32_t wide_mats;        // 1 = every scene's matrix array is 32-byte aligned (256-bit
+                             // matrix loads); set by launch_cull itself for `one_scene`
   CullControl* ctl;
   CullScene one_scene;
   CullView one_view;

@@ -412,6 +412,9 @@ bool launch(dpcull_server s, Slot& slot)
   a.n_items = items;
   a.item_tiles = item_tiles;
   a.items_per_ticket = 1;
+  a.wide_mats = 1;  // 256-bit matrix loads only if every scene's array allows them
+  for (size_t i = 0; i < take.size(); ++i)
+    if ((uintptr_t)slot.h_scenes[i].mats & 31u) a.wide_mats = 0;
   a.ctl = slot.ctl;
   const int occ = cull_max_ctas_per_sm(vpp);
   const long long want = ((long long)items + kWarpsPerCta - 1) / kWarpsPerCta;  // a warp per item

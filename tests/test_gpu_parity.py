@@ -344,6 +344,18 @@ def test_bound_matrices_any_16_byte_alignment(ctx, offset_floats):
     ctx.cull_batched([(g, rs, vps)])
     for rv, (bits, _) in zip(rs, exp):
         assert np.array_equal(ctx.result_bits(rv), bits)
+    # one launch over this group and a group with its own (aligned) copy of the matrices:
+    # the launch takes the 256-bit loads only when both arrays allow them
+    g2 = ctx.group_create()
+    ctx.group_set_objects(g2, lower, extent, xform)
+    ctx.group_set_matrices(g2, mats)
+    rs1 = [ctx.result_create(g) for _ in vps]
+    rs2 = [ctx.result_create(g2) for _ in vps]
+    ctx.cull_batched([(g, rs1, vps), (g2, rs2, vps)])
+    for r1, r2, (bits, _) in zip(rs1, rs2, exp):
+        assert np.array_equal(ctx.result_bits(r1), bits)
+        assert np.array_equal(ctx.result_bits(r2), bits)
+    ctx.group_destroy(g2)
     ctx.group_destroy(g)
     del buf
 
