@@ -205,13 +205,17 @@ __device__ __forceinline__ uint32_t classify_tile(const CullLaunch& a, WarpShare
     // Prefilter boxes of the 4 objects first (their matrix gathers overlap), then each
     // view's planes are read once for all 4 objects.
     pf::Box bx[kObjPerThread];
-    uint32_t valid = 0;
-  #pragma unroll
+    uint32_t valid = 0, bad = 0;
+#pragma unroll
     for (int k = 0; k < kObjPerThread; ++k) {
       const uint32_t mi = compu(xf, k);
       const bool exists = obj0 + k < sc.n_objects;
       const bool use = exists & (mi < sc.n_mats);
-      if (exists && !use && atomicOr(&a.ctl->error, kErrBadTransform) == 0) a.ctl->error_info = obj0 + k;
+      // A transform index past the matrix array is reported and its object skipped.  With
+      // several views one test per tile is cheaper; the 1-view kernel allocates its
+      // registers better with the test per object.
+      if (VPP > 1) bad |= (uint32_t)(exists & !use) << k;
+      else if (exists && !use && atomicOr(&a.ctl->error, kErrBadTransform) == 0) a.ctl->error_info = obj0 + k;
       float4 r0 = make_float4(0.f, 0.f, 0.f, 0.f), r1 = r0, r2 = r0, r3 = r0;
       if (use) load_matrix(sc.mats + 16 * (size_t)mi, WIDE, r0, r1, r2, r3);
       const pf::F4 m0{r0.x, r0.y, r0.z, r0.w}, m1{r1.x, r1.y, r1.z, r1.w};
@@ -219,6 +223,10 @@ __device__ __forceinline__ uint32_t classify_tile(const CullLaunch& a, WarpShare
       bx[k] = pf::make_box(comp(lx, k), comp(ly, k), comp(lz, k), comp(ex, k), comp(ey, k),
                            comp(ez, k), m0, m1, m2, m3);
       valid |= (uint32_t)use << k;
+    }
+    if (VPP > 1 && bad) {
+      const uint32_t o = obj0 + (uint32_t)__ffs(bad) - 1u;
+      if (atomicOr(&a.ctl->error, kErrBadTransform) == 0) a.ctl->error_info = o;
     }
     classify_views(ws, bx, nv, t, valid, amb, lane);
   } else {
