@@ -125,13 +125,34 @@ __device__ __forceinline__ void store_nibble(WarpShared& ws, int v, uint32_t t, 
   if ((lane & 7) == 0) ws.words[v][t][lane >> 3] = w;
 }
 
-// Prefilter of the lane's 4 boxes in each view of the item: visible objects into the
-// tile's words, undecided pairs into amb (bit 8k + v).  Branch-free per pair; the view
-// loop is not unrolled (nv is uniform over the warp).
-__device__ __forceinline__ void classify_views(WarpShared& ws, const pf::Box (&bx)[kObjPerThread],
-                                               int nv, uint32_t t, uint32_t valid, uint32_t& amb,
-                                               int lane)
+// 8x8 transpose of 4-bit elements across the 8 lanes of each lane octet: nibble v of
+// octet lane i moves to nibble i of octet lane v.  Three butterfly steps; in step s the
+// lanes i and i ^ s swap the off-diagonal s x s blocks.
+__device__ __forceinline__ uint32_t transpose_nibbles8(uint32_t x, int lane)
 {
+#pragma unroll
+  for (int s = 1; s <= 4; s <<= 1) {
+    const uint32_t hi = s == 1 ? 0xF0F0F0F0u : s == 2 ? 0xFF00FF00u : 0xFFFF0000u;  // nibble bit set
+    const bool upper = (lane & s) != 0;
+    const uint32_t send = upper ? (x & ~hi) << (4 * s) : (x & hi) >> (4 * s);
+    const uint32_t got = __shfl_xor_sync(0xffffffffu, send, s);
+    x = (upper ? (x & hi) : (x & ~hi)) | got;
+  }
+  return x;
+}
+
+// Prefilter of the lane's 4 boxes in each view of the item; returns the undecided pairs
+// (und_bit<VPP>).  With several views the visible bits collect as nibbles (bit 4v + k:
+// object k, view v) and one nibble transpose per tile gives every lane one visibility
+// word (view lane & 7, word lane >> 3 of the tile): 3 shuffles per tile instead of 3 per
+// view.  With one view the nibble goes to its word directly (the 1-view kernel keeps its
+// registers better that way).  Branch-free per pair; the view loop is not unrolled (nv is
+// uniform over the warp).
+template <int VPP>
+__device__ __forceinline__ uint32_t classify_views(WarpShared& ws, const pf::Box (&bx)[kObjPerThread],
+                                                   int nv, uint32_t t, uint32_t valid, int lane)
+{
+  uint32_t vis_n = 0, und_n = 0;
 #pragma unroll 1
   for (int v = 0; v < nv; ++v) {
     const pf::PlaneRegs P = pf::load_planes(ws.pl[v]);
@@ -143,12 +164,29 @@ __device__ __forceinline__ void classify_views(WarpShared& ws, const pf::Box (&b
       in |= (uint32_t)vis << k;
       und |= (uint32_t)(!vis & !inv) << k;
     }
-    // bit k of und -> bit 8k (the multiply places each bit k at 8k; the mask drops the
-    // cross terms), then view v's column
-    amb |= (((und & valid) * 0x204081u) & 0x01010101u) << v;
-    store_nibble(ws, v, t, in & valid, lane);
+    if (VPP == 1) {
+      // bit k of und -> bit 8k (the multiply places each bit k at 8k; the mask drops the
+      // cross terms)
+      und_n |= ((und & valid) * 0x204081u) & 0x01010101u;
+      store_nibble(ws, v, t, in & valid, lane);
+    } else {
+      vis_n |= in << (4 * v);
+      und_n |= und << (4 * v);
+    }
   }
+  if (VPP == 1) return und_n;
+  const uint32_t vm = valid * 0x11111111u;  // the lane's valid objects in every view
+  const uint32_t w = transpose_nibbles8(vis_n & vm, lane);
+  if ((lane & 7) < nv) ws.words[lane & 7][t][lane >> 3] = w;
+  return und_n & vm;
 }
+
+// Object (within the lane's 4) and view of bit b of classify_views' undecided pairs: bit
+// 8k + v with one view per pass, bit 4v + k with several.
+template <int VPP>
+__device__ __forceinline__ uint32_t und_object(int b) { return VPP == 1 ? (uint32_t)b >> 3 : (uint32_t)b & 3u; }
+template <int VPP>
+__device__ __forceinline__ uint32_t und_view(int b) { return VPP == 1 ? (uint32_t)b & 7u : (uint32_t)b >> 2; }
 
 // Inclusive warp scan.
 __device__ __forceinline__ uint32_t warp_scan(uint32_t x, int lane)
@@ -228,7 +266,7 @@ __device__ __forceinline__ uint32_t classify_tile(const CullLaunch& a, WarpShare
       const uint32_t o = obj0 + (uint32_t)__ffs(bad) - 1u;
       if (atomicOr(&a.ctl->error, kErrBadTransform) == 0) a.ctl->error_info = o;
     }
-    classify_views(ws, bx, nv, t, valid, amb, lane);
+    amb = classify_views<VPP>(ws, bx, nv, t, valid, lane);
   } else {
     // Exact test only: every pair in the reference's operation order (the box is rebuilt
     // per view from the loaded rows; the matrix reloads hit L1).
@@ -269,7 +307,8 @@ __device__ __forceinline__ uint32_t classify_tile(const CullLaunch& a, WarpShare
       uint32_t pos = qn + incl - cnt;
       while (amb) {
         const int b = __ffs(amb) - 1;
-        ws.queue[pos++] = (uint16_t)((t << 10) | ((uint32_t)(lane * kObjPerThread + (b >> 3)) << 3) | (uint32_t)(b & 7));
+        ws.queue[pos++] = (uint16_t)((t << 10) | (((uint32_t)lane * kObjPerThread + und_object<VPP>(b)) << 3) |
+                                     und_view<VPP>(b));
         amb &= amb - 1u;
       }
       qn += tot;
