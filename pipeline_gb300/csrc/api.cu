@@ -87,6 +87,7 @@ struct Result {
   uint32_t* delta = nullptr;        // words_cap: old XOR new visibility (changed-list scratch)
   uint32_t* chunk_tot = nullptr;    // chunks_of(words_cap): changed objects per chunk
   uint32_t n_words = 0;             // visibility words of the group at the last prepare
+  uint32_t last_changed = 0;        // length of the changed list at the last read
 };
 
 struct TreeLaunch {
@@ -153,7 +154,7 @@ struct dpcull_ctx_s {
   cudaStream_t stream = nullptr;
   bool own_stream = false;
   CullControl* ctl = nullptr;
-  unsigned int* h_err = nullptr;     // pinned copy of ctl->error / error_info
+  unsigned int* h_err = nullptr;     // pinned: ctl->error, error_info, one scratch word
   int sm_count = 0;
   uint64_t launches = 0;
   uint64_t device_bytes = 0;
@@ -433,11 +434,17 @@ int stage_upload(dpcull_ctx c, int n, const void* const* src, const size_t* byte
   return DPCULL_OK;
 }
 
-int check_device_errors(dpcull_ctx c)
+// Queues the copy of the device error word pair to c->h_err[0..1]; device_errors_read
+// reports it after the next synchronisation of the stream, so a read of results and its
+// error check share one round trip.
+cudaError_t enqueue_error_read(dpcull_ctx c)
 {
-  CU(cudaMemcpyAsync(c->h_err, &c->ctl->error, 2 * sizeof(unsigned int), cudaMemcpyDeviceToHost,
-                     c->stream));
-  CU(cudaStreamSynchronize(c->stream));
+  return cudaMemcpyAsync(c->h_err, &c->ctl->error, 2 * sizeof(unsigned int), cudaMemcpyDeviceToHost,
+                         c->stream);
+}
+
+int device_errors_read(dpcull_ctx c)
+{
   const unsigned int err = c->h_err[0], info = c->h_err[1];
   if (err) {
     CU(cudaMemsetAsync(&c->ctl->error, 0, 2 * sizeof(unsigned int), c->stream));
@@ -448,6 +455,13 @@ int check_device_errors(dpcull_ctx c)
       return fail(DPCULL_ERR_STATE, "work item %u: a matrix array moved off its 32-byte alignment", info);
   }
   return DPCULL_OK;
+}
+
+int check_device_errors(dpcull_ctx c)
+{
+  CU(enqueue_error_read(c));
+  CU(cudaStreamSynchronize(c->stream));
+  return device_errors_read(c);
 }
 
 int default_vpp(uint32_t max_views)
@@ -661,7 +675,7 @@ int dpcull_ctx_create(int device, void* stream, dpcull_ctx* out)
   }
   CullControl init{};
   e = cudaMemcpy(c->ctl, &init, sizeof init, cudaMemcpyHostToDevice);
-  if (e == cudaSuccess) e = cudaMallocHost((void**)&c->h_err, 2 * sizeof(unsigned int));
+  if (e == cudaSuccess) e = cudaMallocHost((void**)&c->h_err, 4 * sizeof(unsigned int));
   if (e != cudaSuccess) {
     dpcull_ctx_destroy(c);
     return cuda_fail(e, "context set-up");
@@ -1032,17 +1046,23 @@ int dpcull_result_changed(dpcull_ctx c, dpcull_result rh, uint32_t* out, size_t 
 {
   Result* r = get_result(c, rh);
   if (!r || !n) return fail(DPCULL_ERR_INVALID_ARGUMENT, "bad result %u", rh);
-  uint32_t cnt = 0;
-  CU(cudaMemcpyAsync(c->h_err, r->n_changed, 4, cudaMemcpyDeviceToHost, c->stream));
+  // One round trip in the common case: the count, the error word and a prefix of the list
+  // sized from the last read (entries past the count are left unspecified); a second copy
+  // only when the list outgrew the prefix.
+  const size_t spec = out ? std::min<size_t>(cap, std::max<size_t>(4096, r->last_changed + r->last_changed / 2)) : 0;
+  CU(cudaMemcpyAsync(c->h_err + 2, r->n_changed, 4, cudaMemcpyDeviceToHost, c->stream));
+  CU(enqueue_error_read(c));
+  if (spec) CU(cudaMemcpyAsync(out, r->changed, spec * 4, cudaMemcpyDeviceToHost, c->stream));
   CU(cudaStreamSynchronize(c->stream));
-  cnt = c->h_err[0];
-  int rc = check_device_errors(c);
+  const uint32_t cnt = c->h_err[2];
+  int rc = device_errors_read(c);
   if (rc) return rc;
   *n = cnt;
   if (cnt > cap) return fail(DPCULL_ERR_CAPACITY, "changed list has %u entries, buffer %zu", cnt, cap);
-  if (cnt) {
+  r->last_changed = cnt;
+  if (cnt > spec) {
     if (!out) return fail(DPCULL_ERR_INVALID_ARGUMENT, "null output");
-    CU(cudaMemcpyAsync(out, r->changed, (size_t)cnt * 4, cudaMemcpyDeviceToHost, c->stream));
+    CU(cudaMemcpyAsync(out + spec, r->changed + spec, (size_t)(cnt - spec) * 4, cudaMemcpyDeviceToHost, c->stream));
     CU(cudaStreamSynchronize(c->stream));
   }
   return DPCULL_OK;
@@ -1059,8 +1079,9 @@ int dpcull_result_bits(dpcull_ctx c, dpcull_result rh, uint32_t* out, size_t n_w
     if (!out) return fail(DPCULL_ERR_INVALID_ARGUMENT, "null output");
     CU(cudaMemcpyAsync(out, r->bits, words * 4, cudaMemcpyDeviceToHost, c->stream));
   }
+  CU(enqueue_error_read(c));
   CU(cudaStreamSynchronize(c->stream));
-  return check_device_errors(c);
+  return device_errors_read(c);
 }
 
 int dpcull_result_is_visible(dpcull_ctx c, dpcull_result rh, size_t index, int* visible)
@@ -1072,9 +1093,9 @@ int dpcull_result_is_visible(dpcull_ctx c, dpcull_result rh, size_t index, int* 
     return DPCULL_OK;
   }
   uint32_t w = 0;
-  CU(cudaMemcpyAsync(c->h_err, r->bits + index / 32, 4, cudaMemcpyDeviceToHost, c->stream));
+  CU(cudaMemcpyAsync(c->h_err + 2, r->bits + index / 32, 4, cudaMemcpyDeviceToHost, c->stream));
   CU(cudaStreamSynchronize(c->stream));
-  w = c->h_err[0];
+  w = c->h_err[2];
   *visible = (w >> (index % 32)) & 1u;
   return DPCULL_OK;
 }
