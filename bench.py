@@ -407,8 +407,7 @@ def run_plain_config(ctx, args) -> dict:
     for i in range(args.steps):
         t0 = time.perf_counter()
         ctx.cull(g, r, sc["vps"][i % 2])
-        ctx.result_changed(r, changed)
-        ctx.result_bits(r, bits)
+        ctx.result_read(r, bits, changed)  # changed list and visibility words, one call
         lat.append(time.perf_counter() - t0)
     stream = torch.cuda.ExternalStream(ctx.stream)
     ev = _events(torch, 2)

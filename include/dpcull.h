@@ -122,11 +122,20 @@ int dpcull_result_destroy(dpcull_ctx ctx, dpcull_result r);
  * visibility changed since r's previous cull. */
 int dpcull_cull(dpcull_ctx ctx, dpcull_group g, dpcull_result r, const float vp[16]);
 /* Manager::resultGetChanged (Manager.h:129): copies the changed list (group indices,
- * ascending) to host memory; *n receives its length.  DPCULL_ERR_CAPACITY if cap < *n. */
+ * ascending) to host memory; *n receives its length.  DPCULL_ERR_CAPACITY if cap < *n.
+ * Entries of `out` past *n may be overwritten. */
 int dpcull_result_changed(dpcull_ctx ctx, dpcull_result r, uint32_t* out, size_t cap, size_t* n);
 /* Visibility words of r (ceil(n/32) words); *n_bits receives the object count. */
 int dpcull_result_bits(dpcull_ctx ctx, dpcull_result r, uint32_t* out, size_t n_words,
                        size_t* n_bits);
+/* Both reads at once, in one host round trip in the common case: the visibility words
+ * (bits may be NULL to skip; n_words its capacity; *n_bits receives the object count) and
+ * the changed list (changed may be NULL to read the length only; cap its capacity;
+ * *n_changed receives the length).  Entries of `changed` past *n_changed may be
+ * overwritten.  The per-frame read of a reference caller: resultGetChanged plus the
+ * visibility of every object. */
+int dpcull_result_read(dpcull_ctx ctx, dpcull_result r, uint32_t* bits, size_t n_words, size_t* n_bits,
+                       uint32_t* changed, size_t cap, size_t* n_changed);
 /* Manager::resultObjectIsVisible (Manager.h:132) for group index `index`. */
 int dpcull_result_is_visible(dpcull_ctx ctx, dpcull_result r, size_t index, int* visible);
 /* ResultBitSet::onNotify (ResultBitSet.cpp:110-128) for one result: the object that

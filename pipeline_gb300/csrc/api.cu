@@ -1042,30 +1042,44 @@ int dpcull_cull(dpcull_ctx c, dpcull_group gh, dpcull_result rh, const float vp[
   return DPCULL_OK;
 }
 
+// The visibility words (bits: null skips them) and the changed list (n_changed: null skips
+// it; changed: null reads the length only) of one result, in one round trip in the common
+// case: the count, the error word and a prefix of the list sized from the last read
+// travel together (entries past the count are left unspecified); a second copy only when
+// the list outgrew the prefix.  The callers check the words' capacity.
+static int result_read(dpcull_ctx c, Result* r, uint32_t* bits, uint32_t* changed, size_t cap,
+                       size_t* n_changed)
+{
+  const size_t words = (r->size_bits + 31) / 32;
+  if (bits && words) CU(cudaMemcpyAsync(bits, r->bits, words * 4, cudaMemcpyDeviceToHost, c->stream));
+  size_t spec = 0;
+  if (n_changed) {
+    spec = changed ? std::min<size_t>(cap, std::max<size_t>(4096, r->last_changed + r->last_changed / 2)) : 0;
+    CU(cudaMemcpyAsync(c->h_err + 2, r->n_changed, 4, cudaMemcpyDeviceToHost, c->stream));
+    if (spec) CU(cudaMemcpyAsync(changed, r->changed, spec * 4, cudaMemcpyDeviceToHost, c->stream));
+  }
+  CU(enqueue_error_read(c));
+  CU(cudaStreamSynchronize(c->stream));
+  int rc = device_errors_read(c);
+  if (rc || !n_changed) return rc;
+  const uint32_t cnt = c->h_err[2];
+  *n_changed = cnt;
+  if (cnt > cap) return fail(DPCULL_ERR_CAPACITY, "changed list has %u entries, buffer %zu", cnt, cap);
+  r->last_changed = cnt;
+  if (cnt > spec) {
+    if (!changed) return fail(DPCULL_ERR_INVALID_ARGUMENT, "null output");
+    CU(cudaMemcpyAsync(changed + spec, r->changed + spec, (size_t)(cnt - spec) * 4, cudaMemcpyDeviceToHost,
+                       c->stream));
+    CU(cudaStreamSynchronize(c->stream));
+  }
+  return DPCULL_OK;
+}
+
 int dpcull_result_changed(dpcull_ctx c, dpcull_result rh, uint32_t* out, size_t cap, size_t* n)
 {
   Result* r = get_result(c, rh);
   if (!r || !n) return fail(DPCULL_ERR_INVALID_ARGUMENT, "bad result %u", rh);
-  // One round trip in the common case: the count, the error word and a prefix of the list
-  // sized from the last read (entries past the count are left unspecified); a second copy
-  // only when the list outgrew the prefix.
-  const size_t spec = out ? std::min<size_t>(cap, std::max<size_t>(4096, r->last_changed + r->last_changed / 2)) : 0;
-  CU(cudaMemcpyAsync(c->h_err + 2, r->n_changed, 4, cudaMemcpyDeviceToHost, c->stream));
-  CU(enqueue_error_read(c));
-  if (spec) CU(cudaMemcpyAsync(out, r->changed, spec * 4, cudaMemcpyDeviceToHost, c->stream));
-  CU(cudaStreamSynchronize(c->stream));
-  const uint32_t cnt = c->h_err[2];
-  int rc = device_errors_read(c);
-  if (rc) return rc;
-  *n = cnt;
-  if (cnt > cap) return fail(DPCULL_ERR_CAPACITY, "changed list has %u entries, buffer %zu", cnt, cap);
-  r->last_changed = cnt;
-  if (cnt > spec) {
-    if (!out) return fail(DPCULL_ERR_INVALID_ARGUMENT, "null output");
-    CU(cudaMemcpyAsync(out + spec, r->changed + spec, (size_t)(cnt - spec) * 4, cudaMemcpyDeviceToHost, c->stream));
-    CU(cudaStreamSynchronize(c->stream));
-  }
-  return DPCULL_OK;
+  return result_read(c, r, nullptr, out, cap, n);
 }
 
 int dpcull_result_bits(dpcull_ctx c, dpcull_result rh, uint32_t* out, size_t n_words, size_t* n_bits)
@@ -1075,13 +1089,19 @@ int dpcull_result_bits(dpcull_ctx c, dpcull_result rh, uint32_t* out, size_t n_w
   const size_t words = (r->size_bits + 31) / 32;
   if (n_bits) *n_bits = r->size_bits;
   if (words > n_words) return fail(DPCULL_ERR_CAPACITY, "need %zu words", words);
-  if (words) {
-    if (!out) return fail(DPCULL_ERR_INVALID_ARGUMENT, "null output");
-    CU(cudaMemcpyAsync(out, r->bits, words * 4, cudaMemcpyDeviceToHost, c->stream));
-  }
-  CU(enqueue_error_read(c));
-  CU(cudaStreamSynchronize(c->stream));
-  return device_errors_read(c);
+  if (words && !out) return fail(DPCULL_ERR_INVALID_ARGUMENT, "null output");
+  return result_read(c, r, out, nullptr, 0, nullptr);
+}
+
+int dpcull_result_read(dpcull_ctx c, dpcull_result rh, uint32_t* bits, size_t n_words, size_t* n_bits,
+                       uint32_t* changed, size_t cap, size_t* n_changed)
+{
+  Result* r = get_result(c, rh);
+  if (!r || !n_changed) return fail(DPCULL_ERR_INVALID_ARGUMENT, "bad result %u", rh);
+  const size_t words = (r->size_bits + 31) / 32;
+  if (n_bits) *n_bits = r->size_bits;
+  if (bits && words > n_words) return fail(DPCULL_ERR_CAPACITY, "need %zu words", words);
+  return result_read(c, r, bits, changed, cap, n_changed);
 }
 
 int dpcull_result_is_visible(dpcull_ctx c, dpcull_result rh, size_t index, int* visible)

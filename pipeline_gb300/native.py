@@ -74,6 +74,7 @@ _SIGS = {
     "dpcull_cull": (_I, [_P, _U32, _U32, _FP]),
     "dpcull_result_changed": (_I, [_P, _U32, _UP, _SZ, C.POINTER(_SZ)]),
     "dpcull_result_bits": (_I, [_P, _U32, _UP, _SZ, C.POINTER(_SZ)]),
+    "dpcull_result_read": (_I, [_P, _U32, C.c_void_p, _SZ, C.c_void_p, C.c_void_p, _SZ, C.c_void_p]),
     "dpcull_result_is_visible": (_I, [_P, _U32, _SZ, C.POINTER(_I)]),
     "dpcull_result_device": (_I, [_P, _U32, C.POINTER(_P), C.POINTER(_P), C.POINTER(_P)]),
     "dpcull_result_move": (_I, [_P, _U32, _SZ, _SZ]),
@@ -300,6 +301,14 @@ class Context:
         rc = self.lib.dpcull_result_changed(self.h, r, uptr(out), out.shape[0], C.byref(n))
         _check(rc)
         return out[: n.value]
+
+    def result_read(self, r: int, bits: np.ndarray, changed: np.ndarray) -> int:
+        """Visibility words into `bits` and the changed list into `changed` (uint32 arrays
+        large enough) in one call; returns the changed-list length."""
+        nb, nc = _SZ(), _SZ()
+        _check(self.lib.dpcull_result_read(self.h, r, bits.ctypes.data, bits.size, C.byref(nb),
+                                           changed.ctypes.data, changed.size, C.byref(nc)))
+        return nc.value
 
     def result_bits(self, r: int, out: np.ndarray | None = None) -> np.ndarray:
         nb = _SZ()

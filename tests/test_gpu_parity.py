@@ -132,6 +132,31 @@ def test_plain_config_full_size(ctx):
     ctx.group_destroy(g)
 
 
+def test_result_read_one_call(ctx):
+    """dpcull_result_read returns the same words and changed list as the two separate
+    reads, over frames whose changed lists grow past the copied prefix and shrink again."""
+    sc = W.plain_scene(0, 100_000)
+    g = setup_group(ctx, sc["lower"], sc["upper"], sc["xform"], sc["mats"])
+    r = ctx.result_create(g)
+    rng = np.random.default_rng(8)
+    vps = [sc["vps"][0], sc["vps"][1]] + [W.jitter_view(rng, sc["vps"][0], 30.0) for _ in range(3)] + [sc["vps"][0]]
+    exp = port_frames(sc, vps)
+    bits = np.zeros(3125, np.uint32)
+    changed = np.zeros(100_000, np.uint32)
+    for vp, (eb, ec) in zip(vps, exp):
+        ctx.cull(g, r, vp)
+        n = ctx.result_read(r, bits, changed)
+        assert np.array_equal(bits, eb)
+        assert n == len(ec) and np.array_equal(changed[:n], ec)
+    assert max(len(ec) for _, ec in exp) > 4096  # some frame needed the second copy
+    ctx.cull(g, r, vps[1])  # the 1 degree yaw after the first frame again
+    assert len(exp[1][1]) > 1
+    with pytest.raises(native.DpcullError) as e:
+        ctx.result_read(r, bits, np.zeros(1, np.uint32))
+    assert e.value.code == native.ERR_CAPACITY
+    ctx.group_destroy(g)
+
+
 @pytest.mark.parametrize("n", [0, 1, 31, 32, 33, 1023, 1024, 1025, 4097, 70001])
 def test_ragged_sizes(ctx, n):
     rng = np.random.default_rng(n)
