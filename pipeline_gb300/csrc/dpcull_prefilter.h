@@ -232,21 +232,26 @@ DPCULL_HD PlaneRegs load_planes(const Planes& p)
   return PlaneRegs{p.q[0][0], p.q[0][1], p.q[1][0], p.q[1][1], p.q[2][0], p.q[2][1], p.m, p.qf.x};
 }
 
-// The decisions of the comment at the top for one box in one view.
-DPCULL_HD void decide(const Box& b, const PlaneRegs& p, bool& visible, bool& invisible)
+// The decisions of the comment at the top for one box in one view, from its six plane
+// values (lo / hi of x, y, z).
+DPCULL_HD void decide_values(const Box& b, float xl, float xh, float yl, float yh, float zl, float zh,
+                             const F4& m, float qf, bool& visible, bool& invisible)
 {
-  const float xl = plane(b, p.xl), xh = plane(b, p.xh);
-  const float yl = plane(b, p.yl), yh = plane(b, p.yh);
-  const float zl = plane(b, p.zl), zh = plane(b, p.zh);
-  const float da = std::fma(b.d0, p.m.x, p.m.y), db = std::fma(b.d0, p.m.z, p.m.w);
+  const float da = std::fma(b.d0, m.x, m.y), db = std::fma(b.d0, m.z, m.w);
   const float ta = da + b.r;
-  const float uf = std::fma(b.r, p.qf, zh);
+  const float uf = std::fma(b.r, qf, zh);
   const float mlo = std::fmin(std::fmin(xl, yl), zl);
   const float min_in = std::fmin(std::fmin(mlo, xh), yh);
   const float o = std::fmin(mlo, std::fmin(std::fmax(xh, -xl), std::fmax(yh, -yl)));
   // bitwise, not short-circuit: no branches in the kernels
   visible = (min_in > da) & (zh > db);
   invisible = (o <= -ta) | ((uf <= -db) & (zl >= ta));
+}
+
+DPCULL_HD void decide(const Box& b, const PlaneRegs& p, bool& visible, bool& invisible)
+{
+  decide_values(b, plane(b, p.xl), plane(b, p.xh), plane(b, p.yl), plane(b, p.yh), plane(b, p.zl),
+                plane(b, p.zh), p.m, p.qf, visible, invisible);
 }
 
 enum : int { kInvisible = 0, kVisible = 1, kUndecided = 2 };
