@@ -169,8 +169,9 @@ __device__ __forceinline__ uint32_t transpose_nibbles8(uint32_t x, int lane)
 // registers better that way).  The lo and hi planes of an axis are evaluated as one pair
 // (fma.rn.f32x2 on the pairs the view staging interleaved: 9 paired FMAs instead of 18
 // per pair of box and view, each half the same fma.rn.f32 chain as pf::plane), then
-// pf::decide_values decides.  Branch-free per pair; the view loop is not unrolled (nv is
-// uniform over the warp).
+// pf::decide_masks decides (all-ones / zero masks, so each decision becomes its bit with
+// one logic operation).  Branch-free per pair; the view loop is not unrolled (nv is uniform
+// over the warp).
 template <int VPP>
 __device__ __forceinline__ uint32_t classify_views(WarpShared& ws, const pf::Box (&bx)[kObjPerThread],
                                                    int nv, uint32_t t, uint32_t valid, int lane)
@@ -193,10 +194,10 @@ __device__ __forceinline__ uint32_t classify_views(WarpShared& ws, const pf::Box
       upk2(fma2(cz, ax1.x, fma2(cy, ax0.y, fma2(cx, ax0.x, ax1.y))), xl, xh);
       upk2(fma2(cz, ay1.x, fma2(cy, ay0.y, fma2(cx, ay0.x, ay1.y))), yl, yh);
       upk2(fma2(cz, az1.x, fma2(cy, az0.y, fma2(cx, az0.x, az1.y))), zl, zh);
-      bool vis, inv;
-      pf::decide_values(bx[k], xl, xh, yl, yh, zl, zh, m, qf, vis, inv);
-      in |= (uint32_t)vis << k;
-      und |= (uint32_t)(!vis & !inv) << k;
+      uint32_t vis, inv;
+      pf::decide_masks(bx[k], xl, xh, yl, yh, zl, zh, m, qf, vis, inv);
+      in |= vis & (1u << k);
+      und |= ~(vis | inv) & (1u << k);
     }
     if (VPP == 1) {
       // bit k of und -> bit 8k (the multiply places each bit k at 8k; the mask drops the

@@ -232,10 +232,45 @@ DPCULL_HD PlaneRegs load_planes(const Planes& p)
   return PlaneRegs{p.q[0][0], p.q[0][1], p.q[1][0], p.q[1][1], p.q[2][0], p.q[2][1], p.m, p.qf.x};
 }
 
+// All ones when the comparison holds, zero otherwise (false with a NaN operand, like the
+// C++ comparison); on the GPU one set.*.u32.f32 instruction.
+DPCULL_HD uint32_t mask_gt(float a, float b)
+{
+#if defined(__CUDA_ARCH__)
+  uint32_t r;
+  asm("set.gt.u32.f32 %0, %1, %2;" : "=r"(r) : "f"(a), "f"(b));
+  return r;
+#else
+  return a > b ? ~0u : 0u;
+#endif
+}
+
+DPCULL_HD uint32_t mask_le(float a, float b)
+{
+#if defined(__CUDA_ARCH__)
+  uint32_t r;
+  asm("set.le.u32.f32 %0, %1, %2;" : "=r"(r) : "f"(a), "f"(b));
+  return r;
+#else
+  return a <= b ? ~0u : 0u;
+#endif
+}
+
+DPCULL_HD uint32_t mask_ge(float a, float b)
+{
+#if defined(__CUDA_ARCH__)
+  uint32_t r;
+  asm("set.ge.u32.f32 %0, %1, %2;" : "=r"(r) : "f"(a), "f"(b));
+  return r;
+#else
+  return a >= b ? ~0u : 0u;
+#endif
+}
+
 // The decisions of the comment at the top for one box in one view, from its six plane
-// values (lo / hi of x, y, z).
-DPCULL_HD void decide_values(const Box& b, float xl, float xh, float yl, float yh, float zl, float zh,
-                             const F4& m, float qf, bool& visible, bool& invisible)
+// values (lo / hi of x, y, z), as all-ones / zero masks.
+DPCULL_HD void decide_masks(const Box& b, float xl, float xh, float yl, float yh, float zl, float zh,
+                            const F4& m, float qf, uint32_t& visible, uint32_t& invisible)
 {
   const float da = std::fma(b.d0, m.x, m.y), db = std::fma(b.d0, m.z, m.w);
   const float ta = da + b.r;
@@ -243,9 +278,17 @@ DPCULL_HD void decide_values(const Box& b, float xl, float xh, float yl, float y
   const float mlo = std::fmin(std::fmin(xl, yl), zl);
   const float min_in = std::fmin(std::fmin(mlo, xh), yh);
   const float o = std::fmin(mlo, std::fmin(std::fmax(xh, -xl), std::fmax(yh, -yl)));
-  // bitwise, not short-circuit: no branches in the kernels
-  visible = (min_in > da) & (zh > db);
-  invisible = (o <= -ta) | ((uf <= -db) & (zl >= ta));
+  visible = mask_gt(min_in, da) & mask_gt(zh, db);
+  invisible = mask_le(o, -ta) | (mask_le(uf, -db) & mask_ge(zl, ta));
+}
+
+DPCULL_HD void decide_values(const Box& b, float xl, float xh, float yl, float yh, float zl, float zh,
+                             const F4& m, float qf, bool& visible, bool& invisible)
+{
+  uint32_t vis, inv;
+  decide_masks(b, xl, xh, yl, yh, zl, zh, m, qf, vis, inv);
+  visible = vis != 0;
+  invisible = inv != 0;
 }
 
 DPCULL_HD void decide(const Box& b, const PlaneRegs& p, bool& visible, bool& invisible)
