@@ -1594,6 +1594,7 @@ int dpcull_plan_destroy(dpcull_ctx c, dpcull_plan ph)
   Plan* p = get_plan(c, ph);
   if (!p) return fail(DPCULL_ERR_INVALID_ARGUMENT, "bad plan %u", ph);
   cudaStreamSynchronize(c->stream);
+  if (p->copy_stream) cudaStreamSynchronize(p->copy_stream);  // copies into h_counts / snap
   for (int s = 0; s < 2; ++s) {
     if (p->exec[s]) cudaGraphExecDestroy(p->exec[s]);
     if (p->done[s]) cudaEventDestroy(p->done[s]);
@@ -1602,10 +1603,7 @@ int dpcull_plan_destroy(dpcull_ctx c, dpcull_plan ph)
     if (p->h_views[s]) cudaFreeHost(p->h_views[s]);
   }
   if (p->h_counts) cudaFreeHost(p->h_counts);
-  if (p->copy_stream) {
-    cudaStreamSynchronize(p->copy_stream);
-    cudaStreamDestroy(p->copy_stream);
-  }
+  if (p->copy_stream) cudaStreamDestroy(p->copy_stream);
   if (p->snap_ev) cudaEventDestroy(p->snap_ev);
   if (p->counts_ev) cudaEventDestroy(p->counts_ev);
   if (p->copies_ev) cudaEventDestroy(p->copies_ev);
