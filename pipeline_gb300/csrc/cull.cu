@@ -9,11 +9,12 @@
 //      planes in the warp's shared memory, unless the previous item had the same views;
 //   2. per tile: 128-bit streaming loads of the SoA rows (the transform-index row one tile
 //      ahead, so the matrix gathers go out with the other rows); per object, gather its
-//      world matrix (2 x 256-bit loads, or 4 x 128-bit where the array is only 16-byte
-//      aligned) and build its prefilter box; per view, the
-//      conservative prefilter (dpcull_prefilter.h) decides visible / invisible wherever
-//      the reference's rounded result is certain; the decided-visible words go to shared
-//      memory and the undecided (object, view) pairs to the warp's queue;
+//      world matrix (2 x 256-bit loads when the launch's matrix arrays are 32-byte
+//      aligned, else 4 x 128-bit) and build its prefilter box; per view, the conservative
+//      prefilter (dpcull_prefilter.h; an axis' lo and hi plane as one fma.rn.f32x2 pair)
+//      decides visible / invisible wherever the reference's rounded result is certain; the
+//      decided-visible bits go to the item's words in shared memory (one nibble transpose
+//      per tile) and the undecided (object, view) pairs to the warp's queue;
 //   3. all lanes run the queued pairs through the exact reference test (dpcull_exact.cuh)
 //      and set the visible ones in the words;
 //   4. per view of the item: XOR with the result's previous words (ResultBitSet::
@@ -271,8 +272,6 @@ __device__ __forceinline__ uint32_t classify_tile(const CullLaunch& a, WarpShare
   const float4 ex = ld_stream4(soa + 3 * cap + obj0);
   const float4 ey = ld_stream4(soa + 4 * cap + obj0);
   const float4 ez = ld_stream4(soa + 5 * cap + obj0);
-  const float4* mats = reinterpret_cast<const float4*>(sc.mats);
-
   uint32_t amb = 0;
   if (PF) {
     // Prefilter boxes of the 4 objects first (their matrix gathers overlap), then each
@@ -305,6 +304,7 @@ __device__ __forceinline__ uint32_t classify_tile(const CullLaunch& a, WarpShare
   } else {
     // Exact test only: every pair in the reference's operation order (the box is rebuilt
     // per view from the loaded rows; the matrix reloads hit L1).
+    const float4* mats = reinterpret_cast<const float4*>(sc.mats);
     uint32_t use = 0;
 #pragma unroll
     for (int k = 0; k < kObjPerThread; ++k) {
