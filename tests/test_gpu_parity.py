@@ -405,6 +405,49 @@ def test_stress_full_size_eight_views(ctx):
     ctx.group_destroy(g)
 
 
+def test_large_group_repeating_pattern(ctx):
+    """2^28 + 37 objects: a 2^20-object pattern repeated, with a ragged tail.  Checks the
+    index, word and chunk arithmetic at scale through properties that hold at any size:
+    the visibility words repeat with the pattern's period and the first period equals the
+    oracle's; a second frame's changed list is the pattern's list shifted by every period;
+    the batched launch over two views agrees with the plain one."""
+    P, reps, tail = 1 << 20, 256, 37
+    n = P * reps + tail
+    rng = np.random.default_rng(23)
+    lower_p, _, extent_p = W.random_boxes(rng, P)
+    mats = W.random_matrices(rng, 4096)
+    xform_p = rng.integers(0, 4096, P).astype(np.uint32)
+    idx = np.arange(n, dtype=np.int64) % P
+    g = ctx.group_create()
+    ctx.group_set_objects(g, lower_p[:, idx], extent_p[:, idx], xform_p[idx])
+    del idx
+    ctx.group_set_matrices(g, mats)
+    vps = [W.f32([W.perspective()])[0], W.f32([W.rot_y(1.0) @ W.perspective()])[0]]
+    exp = port_frames(dict(lower=lower_p, extent=extent_p, xform=xform_p, mats=mats), vps)
+    wp = P // 32
+    r = ctx.result_create(g)
+    bits = np.zeros((n + 31) // 32, np.uint32)
+    changed = np.zeros(n, np.uint32)
+    for k, vp in enumerate(vps):
+        ctx.cull(g, r, vp)
+        m = ctx.result_read(r, bits, changed)
+        pb, pc = exp[k]
+        assert np.array_equal(bits[: wp * reps].reshape(reps, wp), np.broadcast_to(pb, (reps, wp))), k
+        # the 37 tail objects: one whole word and 5 bits of the last, whose padding is clear
+        assert bits[wp * reps] == pb[0], k
+        assert bits[wp * reps + 1] == (pb[1] & np.uint32(0x1F)), k
+        if k == 1:  # the changed list: every period's changes, then the tail's
+            want = np.concatenate([pc.astype(np.int64) + j * P for j in range(reps)] +
+                                  [pc[pc < tail].astype(np.int64) + reps * P])
+            assert m == want.size and np.array_equal(changed[:m].astype(np.int64), want)
+    rs = [ctx.result_create(g) for _ in vps]
+    ctx.cull_batched([(g, rs, vps)])
+    for rv, vp_bits in zip(rs, [exp[0][0], exp[1][0]]):
+        b = ctx.result_bits(rv)
+        assert np.array_equal(b[: wp * reps].reshape(reps, wp), np.broadcast_to(vp_bits, (reps, wp)))
+    ctx.group_destroy(g)
+
+
 def test_bad_transform_index_is_an_error(ctx):
     rng = np.random.default_rng(1)
     lower, upper, extent = W.random_boxes(rng, 100)
