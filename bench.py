@@ -265,6 +265,7 @@ def run_ours(args, dist: Dist) -> dict | None:
     k_ms = float(np.mean(kernel_ms))
     achieved = bytes_launch / (k_ms / 1e3) / 1e9
     traffic = traffic_from_profile(wl)
+    bounds = issue_roofline(wl, k_ms, (clk or {}).get("sm_mhz"))
     out = {
         "metric": "culled object-views/s (batched persistent launch, bit-exact vs reference CPU manager)",
         "value": value, "unit": "object-views/s", "n_gpus": dist.world, "steps": args.steps,
@@ -285,7 +286,7 @@ def run_ours(args, dist: Dist) -> dict | None:
                      "kernel_ms": k_ms, "step_ms": ms_step,
                      "kernel": "cull_kernel: CUDA events recorded inside the plan graph right before "
                                "and after the kernel, every timed step",
-                     "issue": issue_roofline(wl, k_ms, (clk or {}).get("sm_mhz"))},
+                     "issue": bounds[0], "fp32": bounds[1]},
         "e2e": e2e, "gpu_launches": launches, "clocks": clk, "parity_sample": parity,
         "changed_per_step": changed, "serving": serving_res,
     }
@@ -362,24 +363,42 @@ def traffic_from_profile(wl) -> int | None:
     return _profile_scaled(wl, "dram_bytes_per_launch")
 
 
-def issue_roofline(wl, k_ms: float, sm_mhz) -> dict | None:
-    """The second bound of the cull kernel: warp-instruction issue.  The instruction count
-    per launch comes from the committed ncu capture (scaled by object-views), the duration
-    from this run's in-graph events; the peak is one warp-instruction per scheduler (4 per
-    SM) per cycle at the median SM clock sampled during the timed region."""
+def issue_roofline(wl, k_ms: float, sm_mhz) -> tuple[dict | None, dict | None]:
+    """The cull kernel's compute bounds (pipe_bounds) on this GPU."""
     import torch
 
-    inst = _profile_scaled(wl, "warp_instructions_per_launch")
-    if inst is None or not sm_mhz:
-        return None
     sms = torch.cuda.get_device_properties(torch.cuda.current_device()).multi_processor_count
-    achieved = inst / (k_ms / 1e3) / 1e9
+    return pipe_bounds(wl, k_ms, sm_mhz, sms)
+
+
+def pipe_bounds(wl, k_ms: float, sm_mhz, sms: int) -> tuple[dict | None, dict | None]:
+    """The cull kernel's two compute bounds beside HBM: warp-instruction issue (one per
+    scheduler, 4 per SM, per cycle) and FP32 lane operations (128 lanes per SM per cycle).
+    The counts per launch come from the committed ncu capture (scaled by object-views), the
+    duration from this run's in-graph events, the clock is the median sampled during the
+    timed region."""
+    inst = _profile_scaled(wl, "warp_instructions_per_launch")
+    if inst is None or not sm_mhz or not k_ms:
+        return None, None
+    secs = k_ms / 1e3
+    achieved = inst / secs / 1e9
     peak = sms * 4 * float(sm_mhz) * 1e6 / 1e9
-    return {"bound": "issue", "achieved": achieved, "peak": peak, "unit": "G warp-instructions/s",
-            "frac": achieved / peak, "warp_instructions_per_launch": inst,
-            "thread_instructions_per_object_view": inst * 32 / wl.object_views(),
-            "note": "instruction count from profiles/cull_stress_traffic.json scaled by object-views; "
-                    "peak = SMs x 4 schedulers x median sampled SM clock"}
+    issue = {"bound": "issue", "achieved": achieved, "peak": peak, "unit": "G warp-instructions/s",
+             "frac": achieved / peak, "warp_instructions_per_launch": inst,
+             "thread_instructions_per_object_view": inst * 32 / wl.object_views(),
+             "note": "instruction count from profiles/cull_stress_traffic.json scaled by object-views; "
+                     "peak = SMs x 4 schedulers x median sampled SM clock"}
+    ops = _profile_scaled(wl, "fp32_lane_ops_per_launch")
+    fp32 = None
+    if ops is not None:
+        a = ops / secs / 1e12
+        p = sms * 128 * float(sm_mhz) * 1e6 / 1e12
+        fp32 = {"bound": "fp32", "achieved": a, "peak": p, "unit": "T FP32 lane-ops/s", "frac": a / p,
+                "ops_per_object_view": ops / wl.object_views(),
+                "note": "FFMA, FADD and FMUL count one lane-op, FFMA2 two (ncu opcode counts in "
+                        "profiles/cull_stress_traffic.json); peak = SMs x 128 FP32 lanes x median sampled "
+                        "SM clock"}
+    return issue, fp32
 
 
 # ---- other configurations (separate JSON lines; not the headline) ------------------------------
