@@ -163,7 +163,7 @@ __device__ __forceinline__ uint32_t transpose_nibbles8(uint32_t x, int lane)
 }
 
 // Prefilter of the lane's 4 boxes in each view of the item; returns the undecided pairs
-// (und_bit<VPP>).  With several views the visible bits collect as nibbles (bit 4v + k:
+// (bit layout: und_object / und_view below).  With several views the visible bits collect as nibbles (bit 4v + k:
 // object k, view v) and one nibble transpose per tile gives every lane one visibility
 // word (view lane & 7, word lane >> 3 of the tile): 3 shuffles per tile instead of 3 per
 // view.  With one view the nibble goes to its word directly (the 1-view kernel keeps its
