@@ -24,7 +24,9 @@ import numpy as np
 HERE = Path(__file__).resolve().parent
 PORT_LIB = HERE / "_build" / "liborc.so"
 REF_LIB = HERE / "_ref" / "libdpref.so"
-REF_SRC = Path(os.environ.get("DPCULL_REFERENCE", "/root/reference"))
+# The reference source tree: $DPCULL_REFERENCE, else a checkout named "reference" beside
+# this repository.  Where neither exists the reference build and its tests are skipped.
+REF_SRC = Path(os.environ.get("DPCULL_REFERENCE") or HERE.parent.parent / "reference")
 
 _P, _I, _SZ, _U32, _U64, _I64 = C.c_void_p, C.c_int, C.c_size_t, C.c_uint32, C.c_uint64, C.c_int64
 _FP, _UP, _IP = C.POINTER(C.c_float), C.POINTER(C.c_uint32), C.POINTER(C.c_int)
@@ -81,6 +83,7 @@ _PORT_ONLY = {
     "orc_bounding_box": (None, [_SZ, _FP, _FP, _UP, _FP, _FP, _FP]),
     "orc_propagate": (None, [_SZ, _UP, _FP, _FP, _UP, _UP]),
     "orc_tree_entries": (_SZ, [_P, _UP, _SZ, _UP, _SZ, C.POINTER(_SZ)]),
+    "orc_tree_time_compute": (C.c_double, [_P, _UP, _SZ, _FP, _I, _I]),
 }
 
 _REF_ONLY = {
@@ -341,6 +344,20 @@ def bounding_box(lower, extent, xform, mats):
     a, b = np.zeros(3, np.float32), np.zeros(3, np.float32)
     L.lib.orc_bounding_box(xf.shape[0], fp(lo), fp(ex), up(xf), fp(m), fp(a), fp(b))
     return a, b
+
+
+def time_tree_compute(pairs, locals_, warm: int = 2, reps: int = 10) -> float:
+    """Median ms of the port's Tree::compute after updateLocalMatrix on every transform
+    (the tree built by addTransform in the order of `pairs`, level by level)."""
+    L = port()
+    t = L.tree()
+    for p, x in _u(pairs).reshape(-1, 2):
+        got = t.add(int(p), locals_[x])
+        if got != int(x):
+            raise ValueError("pairs are not in addTransform order")
+    ids = np.arange(1, locals_.shape[0], dtype=np.uint32)
+    m = _f(locals_[1:])
+    return float(L.lib.orc_tree_time_compute(t.h, up(ids), ids.shape[0], fp(m), warm, reps))
 
 
 def propagate(pairs, local, world, dirty_local, dirty_world) -> None:

@@ -5,12 +5,14 @@
  * function names the reference file:line it follows (paths relative to the
  * nvpro-pipeline source tree).  Build with -O2 -ffp-contract=off.
  */
+#define _POSIX_C_SOURCE 199309L /* clock_gettime */
 #include "cull_oracle.h"
 
 #include <float.h>
 #include <pthread.h>
 #include <stdlib.h>
 #include <string.h>
+#include <time.h>
 
 /* ------------------------------------------------------------------------- */
 /* math: dp/math/Matmnt.h:1371-1379 (Vec4 * Mat44) and :1381-1415 (Mat44 * Mat44).
@@ -739,6 +741,33 @@ void orc_tree_compute(orc_tree* t)
   memcpy(t->last_dirty.w, t->dirty_world.w, t->dirty_world.cap_words * sizeof(uint32_t));
   memset(t->dirty_local.w, 0, t->dirty_local.cap_words * sizeof(uint32_t));
   memset(t->dirty_world.w, 0, t->dirty_world.cap_words * sizeof(uint32_t));
+}
+
+/* CPU baseline of the transform propagation: `reps` timed runs (after `warm` untimed
+ * ones) of Tree::compute, each after updateLocalMatrix on the n transforms ids[] (the
+ * per-frame animated case); returns the median milliseconds of compute alone. */
+double orc_tree_time_compute(orc_tree* t, const uint32_t* ids, size_t n, const float* locals, int warm,
+                             int reps)
+{
+  double* ts = (double*)malloc(sizeof(double) * (size_t)(reps > 0 ? reps : 1));
+  int k = 0;
+  for (int i = 0; i < warm + reps; ++i) {
+    for (size_t j = 0; j < n; ++j) orc_tree_update_local(t, ids[j], locals + 16 * j);
+    struct timespec a, b;
+    clock_gettime(CLOCK_MONOTONIC, &a);
+    orc_tree_compute(t);
+    clock_gettime(CLOCK_MONOTONIC, &b);
+    if (i >= warm) ts[k++] = (double)(b.tv_sec - a.tv_sec) * 1e3 + (double)(b.tv_nsec - a.tv_nsec) * 1e-6;
+  }
+  for (int i = 1; i < k; ++i) /* insertion sort: a handful of values */
+    for (int j = i; j > 0 && ts[j - 1] > ts[j]; --j) {
+      double x = ts[j];
+      ts[j] = ts[j - 1];
+      ts[j - 1] = x;
+    }
+  const double med = k ? ts[k / 2] : 0.0;
+  free(ts);
+  return med;
 }
 
 size_t orc_tree_count(orc_tree* t) { return t->capacity; }

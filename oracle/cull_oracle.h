@@ -103,6 +103,9 @@ int64_t orc_tree_add(orc_tree* t, uint32_t parent, const float m[16]); /* -1 whe
 int orc_tree_remove(orc_tree* t, uint32_t index);                      /* -1 where it throws */
 void orc_tree_update_local(orc_tree* t, uint32_t index, const float m[16]);
 void orc_tree_compute(orc_tree* t);
+/* median ms of Tree::compute after updating the n locals ids[] (CPU baseline timing) */
+double orc_tree_time_compute(orc_tree* t, const uint32_t* ids, size_t n, const float* locals, int warm,
+                             int reps);
 size_t orc_tree_count(orc_tree* t);               /* getTransformCount(): the capacity */
 const float* orc_tree_world(orc_tree* t);         /* getWorldMatrices() */
 /* Dirty-world bits delivered by the last compute()'s EventWorldMatricesChanged. */

@@ -299,6 +299,78 @@ DPCULL_HD void decide(const Box& b, const PlaneRegs& p, bool& visible, bool& inv
 
 enum : int { kInvisible = 0, kVisible = 1, kUndecided = 2 };
 
+// ---- decisions against the margin of a group of views -----------------------------------
+// The kernels evaluate up to 8 views per object load.  Instead of each view's own margin
+// classes they use the largest kappa and g over all six planes of every view of the group
+// (K, G): every margin grows, so every decision stays one of the decisions above.  The
+// far plane keeps its normalisation (class B); its radius term R q (q <= 1 + 3.1u) is
+// covered by the class-A inflated radius r'.  Then one pair of thresholds per box serves
+// every plane of every view of the group: D = fl(d0 K + G), T = fl(D + r').
+//   visible   if all six plane values exceed D;
+//   invisible if some lo plane value is <= -T, or for some axis the hi value is <= -T
+//             while the lo value is >= T (max(hi, -lo) <= -T).
+// A view that cannot be bounded gets NaN planes: NaN plane values fail both tests (the
+// minima and maxima of NaNs are NaN), so each of its pairs is undecided whatever the
+// group's margin.
+struct GroupMargin {
+  float k, g;
+};
+
+// The planes of one view for a group decision and the view's contribution to the group
+// margin (0 for a view that cannot be bounded).
+DPCULL_HD bool group_view(const float* vp, Planes& p, GroupMargin& m)
+{
+  const bool ok = make_planes(vp, p);
+  if (ok) {
+    m.k = std::fmax(p.m.x, p.m.z);
+    m.g = std::fmax(p.m.y, p.m.w);
+  } else {
+    const float nan = nan_value();
+    for (int a = 0; a < 3; ++a)
+      for (int h = 0; h < 2; ++h) p.q[a][h] = F4{nan, nan, nan, nan};
+    m.k = 0.f;
+    m.g = 0.f;
+  }
+  return ok;
+}
+
+DPCULL_HD GroupMargin merge(const GroupMargin& a, const GroupMargin& b)
+{
+  return GroupMargin{std::fmax(a.k, b.k), std::fmax(a.g, b.g)};
+}
+
+// Thresholds of one box against a group margin (NaN when the box cannot be bounded).
+DPCULL_HD void group_thresholds(const Box& b, const GroupMargin& m, float& D, float& T)
+{
+  D = std::fma(b.d0, m.k, m.g);
+  T = D + b.r;
+}
+
+// The group decision from the six plane values, as all-ones / zero masks.
+DPCULL_HD void decide_group(float xl, float xh, float yl, float yh, float zl, float zh, float D, float T,
+                            uint32_t& visible, uint32_t& invisible)
+{
+  const float mlo = std::fmin(std::fmin(xl, yl), zl);
+  const float mhi = std::fmin(std::fmin(xh, yh), zh);
+  const float o = std::fmin(std::fmin(mlo, std::fmax(xh, -xl)),
+                            std::fmin(std::fmax(yh, -yl), std::fmax(zh, -zl)));
+  visible = mask_gt(std::fmin(mlo, mhi), D);
+  invisible = mask_le(o, -T);
+}
+
+// Whole classification of one box in one view of a group with margin m.
+DPCULL_HD int classify_group(const Box& b, const Planes& p, const GroupMargin& m)
+{
+  float D, T;
+  group_thresholds(b, m, D, T);
+  uint32_t vis, inv;
+  decide_group(plane(b, p.q[0][0]), plane(b, p.q[0][1]), plane(b, p.q[1][0]), plane(b, p.q[1][1]),
+               plane(b, p.q[2][0]), plane(b, p.q[2][1]), D, T, vis, inv);
+  return vis ? kVisible : inv ? kInvisible : kUndecided;
+}
+
+
+
 // Whole classification of one box in one view (the kernels run decide() with the view's
 // planes loaded once for several boxes).
 DPCULL_HD int classify(const Box& b, const Planes& p)

@@ -98,27 +98,25 @@ def f32(m) -> np.ndarray:
 # ---- objects and transforms ------------------------------------------------------------
 def random_matrices(rng: np.random.Generator, n: int) -> np.ndarray:
     """setMat(q, t, (s,s,s)) (Matmnt.h:527-540): rows 0-2 = s * rotation rows (w = 0),
-    row 3 = (t, 1); q a uniform unit quaternion (normalised 4-D Gaussian)."""
+    row 3 = (t, 1); q a uniform unit quaternion (normalised 4-D Gaussian).  The rotation
+    is evaluated in float64 and each entry rounded once to float32."""
     q = rng.standard_normal((n, 4))
     q /= np.linalg.norm(q, axis=1, keepdims=True)
-    x, y, z, w = q.T
-    R = np.empty((n, 3, 3))
-    R[:, 0, 0] = 1 - 2 * (y * y + z * z)
-    R[:, 0, 1] = 2 * (x * y + z * w)
-    R[:, 0, 2] = 2 * (x * z - y * w)
-    R[:, 1, 0] = 2 * (x * y - z * w)
-    R[:, 1, 1] = 1 - 2 * (x * x + z * z)
-    R[:, 1, 2] = 2 * (y * z + x * w)
-    R[:, 2, 0] = 2 * (x * z + y * w)
-    R[:, 2, 1] = 2 * (y * z - x * w)
-    R[:, 2, 2] = 1 - 2 * (x * x + y * y)
+    x, y, z, w = (np.ascontiguousarray(q[:, i]) for i in range(4))
     s = rng.uniform(0.5, 2.0, n)
     t = rng.uniform(-1000.0, 1000.0, (n, 3))
-    M = np.zeros((n, 4, 4))
-    M[:, :3, :3] = R * s[:, None, None]
-    M[:, 3, :3] = t
-    M[:, 3, 3] = 1.0
-    return M.reshape(n, 16).astype(np.float32)
+    xx, yy, zz = x * x, y * y, z * z
+    xy, xz, yz, zw, yw, xw = x * y, x * z, y * z, z * w, y * w, x * w
+    rot = [1 - 2 * (yy + zz), 2 * (xy + zw), 2 * (xz - yw),
+           2 * (xy - zw), 1 - 2 * (xx + zz), 2 * (yz + xw),
+           2 * (xz + yw), 2 * (yz - xw), 1 - 2 * (xx + yy)]
+    M = np.zeros((n, 16), np.float32)
+    for k, r in enumerate(rot):
+        i, j = divmod(k, 3)
+        M[:, 4 * i + j] = r * s
+    M[:, 12:15] = t
+    M[:, 15] = 1.0
+    return M
 
 
 def random_boxes(rng: np.random.Generator, n: int):
@@ -242,22 +240,33 @@ def scene_views(kind: str, n_views: int) -> list[np.ndarray]:
 
 
 def batched_scenes(seed: int = 2, n_scenes: int = 256, nmin: float = 1e3, nmax: float = 1e6,
-                   scale: float = 1.0):
+                   scale: float = 1.0, workers: int | None = None):
     """Scenes of uneven size (log-uniform object counts) with 1-6 views each:
-    1 view = perspective, 2-4 = shadow cascades, 5-6 = cube faces."""
+    1 view = perspective, 2-4 = shadow cascades, 5-6 = cube faces.  Sizes and view counts
+    come from one generator seeded with `seed`; each scene's boxes and matrices from its
+    own child seed, so the scenes are generated in parallel (`workers` threads)."""
+    import concurrent.futures as cf
+    import os
+
     rng = np.random.default_rng(seed)
-    scenes = []
-    for s in range(n_scenes):
+    sizes, counts = [], []
+    for _ in range(n_scenes):
         n = int(math.floor(math.exp(rng.uniform(math.log(nmin), math.log(nmax))) * scale))
-        n = max(n, 1)
-        v = int(rng.integers(1, 7))
+        sizes.append(max(n, 1))
+        counts.append(int(rng.integers(1, 7)))
+    children = np.random.SeedSequence(seed).spawn(n_scenes)
+
+    def make(k: int) -> dict:
+        r = np.random.default_rng(children[k])
+        n, v = sizes[k], counts[k]
         kind = "perspective" if v == 1 else ("cascades" if v <= 4 else "cube")
-        lower, upper, extent = random_boxes(rng, n)
-        mats = random_matrices(rng, n)
-        scenes.append(dict(lower=lower, upper=upper, extent=extent,
-                           xform=np.arange(n, dtype=np.uint32), mats=mats,
-                           vps=f32(scene_views(kind, v)), kind=kind))
-    return scenes
+        lower, upper, extent = random_boxes(r, n)
+        mats = random_matrices(r, n)
+        return dict(lower=lower, upper=upper, extent=extent, xform=np.arange(n, dtype=np.uint32),
+                    mats=mats, vps=f32(scene_views(kind, v)), kind=kind)
+
+    with cf.ThreadPoolExecutor(max_workers=workers or min(16, os.cpu_count() or 1)) as ex:
+        return list(ex.map(make, range(n_scenes)))
 
 
 def stress_scene(seed: int = 3, n_objects: int = 16_000_000, n_transforms: int = 1_000_000):

@@ -28,6 +28,8 @@ def _build(tmp_path, name, extra=()):
     lib = ctypes.CDLL(str(so))
     lib.pf_classify_soa.argtypes = [ctypes.c_size_t] + [ctypes.c_void_p] * 6
     lib.pf_classify_soa.restype = None
+    lib.pf_classify_group_soa.argtypes = [ctypes.c_size_t] + [ctypes.c_void_p] * 5 + [ctypes.c_size_t, ctypes.c_void_p]
+    lib.pf_classify_group_soa.restype = None
     return lib
 
 
@@ -49,22 +51,39 @@ def classify(lib, lower, extent, xform, mats, vp):
     return out
 
 
+def classify_group(lib, lower, extent, xform, mats, vps):
+    """Every view of vps decided against the group margin of all of them: [views, n]."""
+    n = lower.shape[1]
+    vps = np.ascontiguousarray(np.asarray(vps, np.float32).reshape(-1, 16))
+    out = np.empty((vps.shape[0], n), np.int8)
+    args = [np.ascontiguousarray(a) for a in (lower, extent, xform, mats)]
+    lib.pf_classify_group_soa(n, *[a.ctypes.data for a in args], vps.ctypes.data, vps.shape[0], out.ctypes.data)
+    return out
+
+
 def exact(lower, extent, xform, mats, vp):
     n = lower.shape[1]
     bits = oracle.cull_bits(lower, extent, xform, mats, vp)
     return ((bits[np.arange(n) >> 5] >> (np.arange(n) & 31).astype(np.uint32)) & 1).astype(bool)
 
 
-def check(lib, scene, vps):
-    """Returns (pairs, decided, wrong) over all views."""
+def check(lib, scene, vps, group: int = 8):
+    """Returns (pairs, decided, wrong) over all views: each view decided alone and the
+    views decided in groups of `group` consecutive views against the group margin (as the
+    multi-view kernels do); decided counts the grouped decisions, wrong counts both."""
     pairs = decided = wrong = 0
-    for vp in vps:
+    vps = [np.asarray(v, np.float32).reshape(16) for v in vps]
+    ex = [exact(*scene, vp) for vp in vps]
+    for vp, e in zip(vps, ex):
         cls = classify(lib, *scene, vp)
-        ex = exact(*scene, vp)
-        dec = cls != 2
-        wrong += int(np.count_nonzero(dec & ((cls == 1) != ex)))
-        pairs += cls.size
-        decided += int(np.count_nonzero(dec))
+        wrong += int(np.count_nonzero((cls != 2) & ((cls == 1) != e)))
+    for g0 in range(0, len(vps), group):
+        cls = classify_group(lib, *scene, vps[g0:g0 + group])
+        for k, c in enumerate(cls):
+            dec = c != 2
+            wrong += int(np.count_nonzero(dec & ((c == 1) != ex[g0 + k])))
+            pairs += c.size
+            decided += int(np.count_nonzero(dec))
     return pairs, decided, wrong
 
 
@@ -196,3 +215,42 @@ def test_weak_margin_is_caught(pf_weak):
         pts = points_on_planes(rng, vp, n, (0.2, 4000.0))
         wrong += check(pf_weak, boxes_scene(rng, n, pts, (1e-7, 1e-5)), [vp])[2]
     assert wrong > 0
+
+
+def test_group_with_an_unbounded_view(pf):
+    """A view that cannot be bounded (a non-finite entry) in a group: its pairs are all
+    undecided, the other views of the group still decide nearly every pair."""
+    rng = np.random.default_rng(16)
+    n = 30_000
+    lower, _, extent = wl.random_boxes(rng, n)
+    mats = wl.random_matrices(rng, 2048)
+    xform = rng.integers(0, 2048, n).astype(np.uint32)
+    scene = (lower, extent, xform, mats)
+    vps = [np.asarray(v, np.float32).reshape(16) for v in wl.cube_face_views() + wl.stereo_views()]
+    vps[3] = vps[3].copy()
+    vps[3][5] = np.inf
+    cls = classify_group(pf, *scene, vps)
+    assert np.all(cls[3] == 2)
+    for k in (0, 1, 2, 4, 5, 6, 7):
+        e = exact(*scene, vps[k])
+        dec = cls[k] != 2
+        assert not np.any(dec & ((cls[k] == 1) != e))
+        assert np.count_nonzero(dec) >= 0.98 * n
+
+
+def test_group_margin_is_the_largest(pf):
+    """A group's decisions are never looser than any member's own: wherever a view decides
+    a pair inside the group, it decides it the same way alone."""
+    rng = np.random.default_rng(17)
+    n = 30_000
+    lower, _, extent = wl.random_boxes(rng, n)
+    mats = wl.random_matrices(rng, 2048)
+    xform = rng.integers(0, 2048, n).astype(np.uint32)
+    scene = (lower, extent, xform, mats)
+    vps = [np.asarray(v, np.float32).reshape(16)
+           for v in wl.cube_face_views()[:3] + wl.cascade_views()[:3] + wl.stereo_views()]
+    cls = classify_group(pf, *scene, vps)
+    for k, vp in enumerate(vps):
+        alone = classify(pf, *scene, vp)
+        dec = cls[k] != 2
+        assert np.array_equal(cls[k][dec], alone[dec])
