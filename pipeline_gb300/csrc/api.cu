@@ -126,7 +126,9 @@ struct Plan {
   bool fresh[2] = {false, false};      // slot holds matrices from set_views
   std::vector<uint32_t> all_groups;    // every job's group (empty ones included)
   std::vector<uint32_t> all_results;   // every job's results, in job and view order
-  uint32_t* h_counts = nullptr;        // pinned: changed counts read by dpcull_plan_read
+  uint32_t* h_counts = nullptr;        // pinned: changed counts of the snapshot (read_async)
+  uint32_t* h_rcounts = nullptr;       // pinned: changed counts read by dpcull_plan_read, apart
+                                       // from a pending snapshot's, which it must not overwrite
   // dpcull_plan_read_async: device snapshots of the results, copied out on copy_stream
   cudaStream_t copy_stream = nullptr;
   cudaEvent_t snap_ev = nullptr, counts_ev = nullptr, copies_ev = nullptr;
@@ -1327,6 +1329,7 @@ int dpcull_plan_create(dpcull_ctx c, const dpcull_job* jobs, size_t n_jobs,
     for (uint32_t v = 0; v < jobs[j].n_views; ++v) p.all_results.push_back(jobs[j].results[v]);
   }
   CU(cudaMallocHost((void**)&p.h_counts, (p.all_results.size() + 2) * sizeof(uint32_t)));
+  CU(cudaMallocHost((void**)&p.h_rcounts, (p.all_results.size() + 2) * sizeof(uint32_t)));
   rc = dalloc(c, (void**)&p.d_scenes, p.scenes.size() * sizeof(CullScene));
   if (!rc) rc = dalloc(c, (void**)&p.d_views, p.views.size() * sizeof(CullView));
   if (rc) return rc;
@@ -1418,16 +1421,17 @@ int dpcull_plan_read(dpcull_ctx c, dpcull_plan ph, uint32_t* const* bits, uint32
     rs[i] = get_result(c, p->all_results[i]);
     if (!rs[i]) return fail(DPCULL_ERR_STATE, "plan %u: result %u was destroyed", ph, p->all_results[i]);
   }
-  // 1. every changed count and the device error word, one wait
+  // 1. every changed count and the device error word, one wait (into a buffer of its own:
+  //    a snapshot taken before this read keeps its counts for dpcull_plan_read_async)
   for (size_t i = 0; i < nr; ++i)
-    CU(cudaMemcpyAsync(p->h_counts + i, rs[i]->n_changed, 4, cudaMemcpyDeviceToHost, c->stream));
-  CU(cudaMemcpyAsync(p->h_counts + nr, &c->ctl->error, 2 * sizeof(unsigned int), cudaMemcpyDeviceToHost,
+    CU(cudaMemcpyAsync(p->h_rcounts + i, rs[i]->n_changed, 4, cudaMemcpyDeviceToHost, c->stream));
+  CU(cudaMemcpyAsync(p->h_rcounts + nr, &c->ctl->error, 2 * sizeof(unsigned int), cudaMemcpyDeviceToHost,
                      c->stream));
   CU(cudaStreamSynchronize(c->stream));
-  if (p->h_counts[nr]) return check_device_errors(c);
+  if (p->h_rcounts[nr]) return check_device_errors(c);
   // 2. every requested array, one wait
   for (size_t i = 0; i < nr; ++i) {
-    const uint32_t cnt = p->h_counts[i];
+    const uint32_t cnt = p->h_rcounts[i];
     if (n_changed) n_changed[i] = cnt;
     if (bits && bits[i] && rs[i]->size_bits)
       CU(cudaMemcpyAsync(bits[i], rs[i]->bits, (rs[i]->size_bits + 31) / 32 * 4, cudaMemcpyDeviceToHost,
@@ -1603,6 +1607,7 @@ int dpcull_plan_destroy(dpcull_ctx c, dpcull_plan ph)
     if (p->h_views[s]) cudaFreeHost(p->h_views[s]);
   }
   if (p->h_counts) cudaFreeHost(p->h_counts);
+  if (p->h_rcounts) cudaFreeHost(p->h_rcounts);
   if (p->copy_stream) cudaStreamDestroy(p->copy_stream);
   if (p->snap_ev) cudaEventDestroy(p->snap_ev);
   if (p->counts_ev) cudaEventDestroy(p->counts_ev);

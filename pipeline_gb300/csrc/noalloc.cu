@@ -13,11 +13,15 @@
 //
 // The array lives in every GPU that loads this library until the process exits
 // (about 128 KB).  Its device address is looked up once per device, with that device
-// current, on the first call made on the device; make that first call before any
-// stream capture.  All calls share the array and it keeps the last call's contents:
-// each call clears the parts that must start at zero, and calls whose work overlaps on
-// the GPU (on different streams, or on one stream from several host threads without
-// ordering) race on it.
+// current, on the first call made on the device, and kept for the life of the process;
+// make that first call before any stream capture.  cudaDeviceReset destroys the array
+// together with the device's context, so after a reset of a device this entry point
+// must not be called on it again in the same process (the kept address would name
+// memory of the old context).  All calls share the array and it keeps the last call's
+// contents: each call clears the parts that must start at zero, and calls whose work
+// overlaps on the GPU (on different streams, or on one stream from several host threads
+// without ordering) race on it.  Each call waits for its own work on the stream
+// (cudaStreamSynchronize) before it returns.
 #include <cuda_runtime.h>
 
 #include <cstdint>

@@ -86,6 +86,7 @@ struct Slot {
   uint32_t* h_counts = nullptr;   // pinned, one per view
   bool busy = false;
   std::vector<Request> reqs;
+  std::vector<Scene*> scn;        // the scene of each request, looked up under the scenes lock
   std::vector<size_t> bits_off;   // per request: word offset of its first view's bits
   uint32_t* d_out = nullptr;
   size_t out_bytes = 0;
@@ -109,7 +110,10 @@ struct dpcull_server_s {
   Slot slots[kMaxStreams];
 
   std::mutex scenes_mu;      // residency state; the worker holds it across CUDA calls
-  std::deque<Scene> scenes;  // references stay valid as scenes are added
+  // Scenes by id.  dpcull_server_add_scene may grow the deque at any time (under
+  // scenes_mu): references to its elements stay valid, but indexing it is only safe under
+  // the lock, so the worker indexes it under the lock and keeps Scene pointers.
+  std::deque<Scene> scenes;
   std::list<uint32_t> lru;   // resident scenes, least recently used first
   cudaStream_t up_stream = nullptr;  // scene uploads and evictions
   // What a submit checks (registered, size), under a lock the worker never takes, so a
@@ -216,7 +220,7 @@ void retire(dpcull_server s, Slot& slot)
   size_t v0 = 0;
   for (size_t i = 0; i < slot.reqs.size(); ++i) {
     const Request& q = slot.reqs[i];
-    Scene& sc = s->scenes[q.scene];
+    Scene& sc = *slot.scn[i];
     sc.pending--;
     dpcull_completion c{};
     c.request = q.id;
@@ -233,12 +237,10 @@ void retire(dpcull_server s, Slot& slot)
   }
   {
     std::lock_guard<std::mutex> lk(s->done_mu);
-    size_t off = 0;
     for (auto& k : slot.kept) {
-      (void)off;
       auto it = std::find_if(slot.reqs.begin(), slot.reqs.end(), [&](const Request& r) { return r.id == k.id; });
       const Request& q = *it;
-      const size_t words = s->scenes[q.scene].cap / 32;
+      const size_t words = slot.scn[it - slot.reqs.begin()]->cap / 32;
       std::vector<std::vector<uint32_t>> views(q.n_views);
       for (uint32_t v = 0; v < q.n_views; ++v)
         views[v].assign(k.words.begin() + v * words, k.words.begin() + (v + 1) * words);
@@ -249,6 +251,7 @@ void retire(dpcull_server s, Slot& slot)
   s->inflight_bytes -= slot.out_bytes;
   s->completed += slot.reqs.size();
   slot.reqs.clear();
+  slot.scn.clear();
   slot.kept.clear();
   slot.busy = false;
 }
@@ -282,6 +285,7 @@ void start_uploads(dpcull_server s, const std::vector<uint32_t>& missing)
 bool launch(dpcull_server s, Slot& slot)
 {
   std::vector<Request> take;
+  std::vector<Scene*> take_sc;  // Scene of each taken request (stable while the server lives)
   std::vector<uint32_t> missing;
   uint64_t work = 0, out_bytes = 0;
   uint32_t max_views = 1;
@@ -336,6 +340,7 @@ bool launch(dpcull_server s, Slot& slot)
       work += w;
       max_views = std::max(max_views, q.n_views);
       take.push_back(q);
+      take_sc.push_back(&sc);
     }
   }
   if (!left.empty()) {
@@ -358,8 +363,8 @@ bool launch(dpcull_server s, Slot& slot)
 
   const int vpp = vpp_for(max_views);
   uint64_t tile_groups = 0;
-  for (auto& q : take)
-    tile_groups += (s->scenes[q.scene].cap / kTileObjects) * (uint64_t)((q.n_views + vpp - 1) / vpp);
+  for (size_t i = 0; i < take.size(); ++i)
+    tile_groups += (take_sc[i]->cap / kTileObjects) * (uint64_t)((take[i].n_views + vpp - 1) / vpp);
   const uint32_t item_tiles = item_tiles_for(tile_groups, s->sm_count);
   uint32_t items = 0, max_tiles = 1, vi = 0;
   size_t kept_words = 0;
@@ -372,7 +377,7 @@ bool launch(dpcull_server s, Slot& slot)
   slot.d_views = reinterpret_cast<CullView*>(reinterpret_cast<char*>(slot.d_scenes) + voff);
   for (size_t i = 0; i < take.size(); ++i) {
     const Request& q = take[i];
-    Scene& sc = s->scenes[q.scene];
+    const Scene& sc = *take_sc[i];
     CullScene cs{};
     cs.soa = sc.dev;
     cs.mats = sc.dev + 7 * sc.cap;
@@ -430,7 +435,7 @@ bool launch(dpcull_server s, Slot& slot)
     size_t off = 0;
     for (size_t i = 0; i < take.size(); ++i)
       if (take[i].flags & DPCULL_REQUEST_KEEP_BITS) {
-        const size_t w = take[i].n_views * (s->scenes[take[i].scene].cap / 32);
+        const size_t w = take[i].n_views * (take_sc[i]->cap / 32);
         cudaMemcpyAsync(slot.kept_pinned + off, slot.d_out + slot.bits_off[i], w * 4, cudaMemcpyDeviceToHost, slot.stream);
         off += w;
       }
@@ -439,6 +444,7 @@ bool launch(dpcull_server s, Slot& slot)
   slot.d_out = nullptr;
   cudaEventRecord(slot.done, slot.stream);
   slot.reqs = std::move(take);
+  slot.scn = std::move(take_sc);
   slot.start_s = now_s();
   slot.busy = true;
   s->stats.batches++;
@@ -601,7 +607,8 @@ int dpcull_server_add_scene(dpcull_server s, uint32_t scene, size_t n, const flo
     return record_error(DPCULL_ERR_OUT_OF_RANGE, "dpcull_server_add_scene: transform index past the matrices");
   if (scene >= s->scenes.size()) {
     if (scene > 16u * 1024u * 1024u) return record_error(DPCULL_ERR_INVALID_ARGUMENT, "scene id too large");
-    // The worker holds no references into the vector while this lock is held.
+    // Growing the deque keeps every Scene where it is: the worker's Scene pointers stay
+    // valid, and it only indexes the deque under this lock.
     s->scenes.resize(scene + 1);
   }
   Scene& sc = s->scenes[scene];

@@ -291,6 +291,51 @@ def test_plan_snapshot_pipelined_frames(ctx):
     ctx.group_destroy(g)
 
 
+def test_plan_read_between_snapshot_and_async_read(ctx):
+    """snapshot of frame 0, launch of frame 1, dpcull_plan_read (frame 1), then
+    dpcull_plan_read_async: the blocking read returns frame 1 and the asynchronous read
+    still returns the snapshot of frame 0, words and changed lists with their own counts."""
+    n, nv = 100_003, 4
+    sc = W.stress_scene(seed=13, n_objects=n, n_transforms=5000)
+    g = setup_group(ctx, sc["lower"], sc["upper"], sc["xform"], sc["mats"])
+    rs = [ctx.result_create(g) for _ in range(nv)]
+    p = ctx.plan_create([(g, rs, sc["vps"][:nv])], dict(views_per_pass=4, tiles_per_ticket=1, ctas_per_sm=0))
+    rng = np.random.default_rng(14)
+    f0 = sc["vps"][:nv]
+    f1 = np.stack([W.jitter_view(rng, v, 25.0) for v in f0])
+    obbs = oracle.build_obbs(sc["lower"], sc["extent"], sc["xform"], sc["mats"])
+    prev = [np.full((n + 31) // 32, 0xFFFFFFFF, np.uint32) for _ in range(nv)]
+    for w in prev:
+        w[-1] = (1 << (n % 32)) - 1
+    expect = []
+    for vps in (f0, f1):
+        fr = []
+        for v in range(nv):
+            bits = oracle.cull_obbs(obbs, vps[v], threads=8)
+            fr.append((bits, oracle.update_changed(prev[v], bits, n)))
+        expect.append(fr)
+    assert any(len(expect[0][v][1]) != len(expect[1][v][1]) for v in range(nv))
+    bits0 = [np.zeros((n + 31) // 32, np.uint32) for _ in range(nv)]
+    ch0 = [np.zeros(n, np.uint32) for _ in range(nv)]
+    bits1 = [np.zeros((n + 31) // 32, np.uint32) for _ in range(nv)]
+    ch1 = [np.zeros(n, np.uint32) for _ in range(nv)]
+    ctx.plan_set_views(p, f0)
+    ctx.plan_launch(p)
+    ctx.plan_snapshot(p)
+    ctx.plan_set_views(p, f1)
+    ctx.plan_launch(p)
+    n1 = ctx.plan_read(p, bits1, ch1)
+    n0 = ctx.plan_read_async(p, bits0, ch0)
+    ctx.plan_read_wait(p)
+    for k, (nk, bk, ck) in enumerate(((n0, bits0, ch0), (n1, bits1, ch1))):
+        for v in range(nv):
+            eb, ec = expect[k][v]
+            assert np.array_equal(bk[v], eb), (k, v)
+            assert nk[v] == len(ec) and np.array_equal(ck[v][: len(ec)], ec), (k, v)
+    ctx.plan_destroy(p)
+    ctx.group_destroy(g)
+
+
 def test_plan_autotuned(ctx, tmp_path, monkeypatch):
     sc = W.stress_scene(seed=10, n_objects=200_000, n_transforms=5000)
     g = setup_group(ctx, sc["lower"], sc["upper"], sc["xform"], sc["mats"])

@@ -72,3 +72,54 @@ def test_submit_rejects_what_cannot_fit(ctx):
         with pytest.raises(native.DpcullError) as e:
             srv.submit(0, W.f32([W.perspective()]))
         assert e.value.code == native.ERR_CAPACITY
+
+
+def test_scenes_added_while_serving(ctx):
+    """Scenes with growing ids are registered from another thread while requests on the
+    first scenes are admitted, launched and retired: the catalogue grows under the
+    scheduler without disturbing it, and every result is still the oracle's."""
+    import threading
+
+    templates = serving.make_templates(seed=6, n_templates=3, nmin=2_000, nmax=40_000)
+    rng = np.random.default_rng(10)
+    reqs = []
+    for _ in range(200):
+        scene = int(rng.integers(0, 3))
+        vps = W.f32(W.cube_face_views(rng.uniform(-20, 20, 3)))[: int(rng.integers(1, 7))]
+        reqs.append((scene, vps))
+    with native.Server(ctx, 1 << 30, n_streams=3, max_batch_objects=1 << 20) as srv:
+        for k in range(3):
+            t = templates[k]
+            srv.add_scene(k, t["lower"], t["extent"], t["xform"], t["mats"])
+        errors = []
+
+        def add_more():
+            try:
+                for k in range(3, 3000):  # ids grow one by one: the scene table keeps growing
+                    t = templates[k % 3]
+                    srv.add_scene(k, t["lower"], t["extent"], t["xform"], t["mats"])
+            except Exception as e:  # pragma: no cover - reported below
+                errors.append(e)
+
+        th = threading.Thread(target=add_more)
+        th.start()
+        ids, sent = [], []
+        while th.is_alive() or len(ids) < len(reqs):  # requests flow while the table grows
+            scene, vps = reqs[len(ids) % len(reqs)]
+            keep = len(ids) % 7 == 0
+            ids.append(srv.submit(scene, vps, keep_bits=keep))
+            sent.append((scene, vps, keep))
+        th.join()
+        srv.drain()
+        assert not errors
+        comps = {c[0]: c for c in srv.poll()}
+        assert len(comps) == len(ids)
+        for rid, (scene, vps, keep) in zip(ids, sent):
+            if not keep:
+                continue
+            t = templates[scene]
+            words = -(-t["n"] // 1024) * 32
+            for v, vp in enumerate(vps):
+                got = srv.result(rid, v, words)[: (t["n"] + 31) // 32]
+                assert np.array_equal(got, oracle.cull_bits(t["lower"], t["extent"], t["xform"], t["mats"], vp))
+
