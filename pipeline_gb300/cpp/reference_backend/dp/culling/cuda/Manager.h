@@ -21,6 +21,13 @@ namespace dp
       public:
         // device: CUDA ordinal of the GPU to cull on.
         DP_CULLING_API static Manager* create( int device = 0 );
+
+        // Culls the group against `count` world matrices already in device memory (16-byte
+        // aligned, 16 floats each, for instance the output of a GPU transform tree) instead
+        // of the host array of groupSetMatrices: no host round trip, the matrices are read
+        // at every cull.  nullptr returns the group to its host matrices.
+        DP_CULLING_API virtual void groupSetDeviceMatrices( GroupSharedPtr const& group, float const* matrices,
+                                                            size_t count ) = 0;
       };
 
     } // namespace cuda
