@@ -59,7 +59,7 @@ __device__ __forceinline__ uint32_t compu(const uint4& v, int k)
 struct WarpShared {
   CullScene sc;                                          // the scene of the warp's last item
   CullView cv[kMaxViewsPerPass];                         // the item's views (matrices + outputs)
-  pf::Planes pl[kMaxViewsPerPass];                       // prefilter planes of the views
+  pf::GroupMargin gm;                                    // margin of the staged view group
   uint32_t words[kMaxViewsPerPass][kItemTiles][kTileWords];  // the item's visibility words
   uint16_t queue[kQueueCap];                             // tile << 10 | object << 3 | view
   ulonglong2 qp[kMaxViewsPerPass][3][2];                 // per axis: (lo, hi) pairs of x, y | z, w
@@ -170,36 +170,46 @@ __device__ __forceinline__ uint32_t transpose_nibbles8(uint32_t x, int lane)
 // registers better that way).  The lo and hi planes of an axis are evaluated as one pair
 // (fma.rn.f32x2 on the pairs the view staging interleaved: 9 paired FMAs instead of 18
 // per pair of box and view, each half the same fma.rn.f32 chain as pf::plane), then
-// pf::decide_masks decides (all-ones / zero masks, so each decision becomes its bit with
-// one logic operation).  Branch-free per pair; the view loop is not unrolled (nv is uniform
-// over the warp).
+// pf::decide_group decides against the view group's margin (each box's two thresholds
+// are computed once for all the group's views; all-ones / zero masks, so each decision
+// becomes its bit with one logic operation).  Branch-free per pair; the view loop is not
+// unrolled (nv is uniform over the warp).
 template <int VPP>
 __device__ __forceinline__ uint32_t classify_views(WarpShared& ws, const pf::Box (&bx)[kObjPerThread],
                                                    int nv, uint32_t t, uint32_t valid, int lane)
 {
+  // Per box: its centre as (c, c) pairs and its two thresholds against the group margin,
+  // once for all views.
+  unsigned long long cx[kObjPerThread], cy[kObjPerThread], cz[kObjPerThread];
+  float D[kObjPerThread], T[kObjPerThread];
+  const pf::GroupMargin gm = ws.gm;
+#pragma unroll
+  for (int k = 0; k < kObjPerThread; ++k) {
+    cx[k] = pk2(bx[k].cx, bx[k].cx);
+    cy[k] = pk2(bx[k].cy, bx[k].cy);
+    cz[k] = pk2(bx[k].cz, bx[k].cz);
+    pf::group_thresholds(bx[k], gm, D[k], T[k]);
+  }
   uint32_t vis_n = 0, und_n = 0;
 #pragma unroll 1
   for (int v = 0; v < nv; ++v) {
     const ulonglong2 ax0 = ws.qp[v][0][0], ax1 = ws.qp[v][0][1];
     const ulonglong2 ay0 = ws.qp[v][1][0], ay1 = ws.qp[v][1][1];
     const ulonglong2 az0 = ws.qp[v][2][0], az1 = ws.qp[v][2][1];
-    const pf::F4 m = ws.pl[v].m;
-    const float qf = ws.pl[v].qf.x;
-    uint32_t in = 0, und = 0;
+    uint32_t in = 0, out = 0;
 #pragma unroll
     for (int k = 0; k < kObjPerThread; ++k) {
       // each axis' lo and hi plane values as one pair (the FMA chain of pf::plane)
-      const unsigned long long cx = pk2(bx[k].cx, bx[k].cx), cy = pk2(bx[k].cy, bx[k].cy);
-      const unsigned long long cz = pk2(bx[k].cz, bx[k].cz);
       float xl, xh, yl, yh, zl, zh;
-      upk2(fma2(cz, ax1.x, fma2(cy, ax0.y, fma2(cx, ax0.x, ax1.y))), xl, xh);
-      upk2(fma2(cz, ay1.x, fma2(cy, ay0.y, fma2(cx, ay0.x, ay1.y))), yl, yh);
-      upk2(fma2(cz, az1.x, fma2(cy, az0.y, fma2(cx, az0.x, az1.y))), zl, zh);
+      upk2(fma2(cz[k], ax1.x, fma2(cy[k], ax0.y, fma2(cx[k], ax0.x, ax1.y))), xl, xh);
+      upk2(fma2(cz[k], ay1.x, fma2(cy[k], ay0.y, fma2(cx[k], ay0.x, ay1.y))), yl, yh);
+      upk2(fma2(cz[k], az1.x, fma2(cy[k], az0.y, fma2(cx[k], az0.x, az1.y))), zl, zh);
       uint32_t vis, inv;
-      pf::decide_masks(bx[k], xl, xh, yl, yh, zl, zh, m, qf, vis, inv);
+      pf::decide_group(xl, xh, yl, yh, zl, zh, D[k], T[k], vis, inv);
       in |= vis & (1u << k);
-      und |= ~(vis | inv) & (1u << k);
+      out |= inv & (1u << k);
     }
+    const uint32_t und = ~(in | out) & 0xFu;
     if (VPP == 1) {
       // bit k of und -> bit 8k (the multiply places each bit k at 8k; the mask drops the
       // cross terms)
@@ -428,14 +438,22 @@ __device__ __forceinline__ void warp_item(const CullLaunch& a, uint32_t item, Wa
     const uint32_t* src = reinterpret_cast<const uint32_t*>(a.views ? a.views + key : &a.one_view);
     for (int i = lane; i < nv * kViewWords; i += 32) reinterpret_cast<uint32_t*>(ws.cv)[i] = src[i];
     __syncwarp();
-    if (PF && lane < nv) {
-      pf::make_planes(ws.cv[lane].vp, ws.pl[lane]);
-      const pf::Planes& pl = ws.pl[lane];
-      for (int ax = 0; ax < 3; ++ax) {
-        const pf::F4 lo = pl.q[ax][0], hi = pl.q[ax][1];
-        ws.qp[lane][ax][0] = make_ulonglong2(pk2(lo.x, hi.x), pk2(lo.y, hi.y));
-        ws.qp[lane][ax][1] = make_ulonglong2(pk2(lo.z, hi.z), pk2(lo.w, hi.w));
+    if (PF) {
+      pf::GroupMargin m{0.f, 0.f};
+      if (lane < nv) {
+        pf::Planes pl;
+        pf::group_view(ws.cv[lane].vp, pl, m);
+        for (int ax = 0; ax < 3; ++ax) {
+          const pf::F4 lo = pl.q[ax][0], hi = pl.q[ax][1];
+          ws.qp[lane][ax][0] = make_ulonglong2(pk2(lo.x, hi.x), pk2(lo.y, hi.y));
+          ws.qp[lane][ax][1] = make_ulonglong2(pk2(lo.z, hi.z), pk2(lo.w, hi.w));
+        }
       }
+      // the group margin: the largest over the views (lanes past nv contribute zeros)
+#pragma unroll
+      for (int d = 1; d < kMaxViewsPerPass; d <<= 1)
+        m = pf::merge(m, pf::GroupMargin{__shfl_xor_sync(0xffffffffu, m.k, d), __shfl_xor_sync(0xffffffffu, m.g, d)});
+      if (lane == 0) ws.gm = m;
     }
     __syncwarp();
     vkey = key;
