@@ -74,6 +74,16 @@ uint64_t dpcull_ctx_device_bytes(dpcull_ctx ctx);
  * way: the prefilter only decides object-views whose outcome is certain under the
  * reference's rounding and sends all others through the exact test. */
 int dpcull_ctx_set_prefilter(dpcull_ctx ctx, int enabled);
+/* Whether groups keep their boxes between culls (default: on), as the reference keeps its
+ * OBB cache between culls (GroupCPU::updateOBBs, dp/culling/cpu/src/ManagerImpl.cpp:
+ * 114-162).  A group culled again with unchanged objects and matrices has its prefilter
+ * boxes (20 bytes per object) and OBBs (64 bytes per object) stored by that cull, and every
+ * later cull reads them instead of the objects and their world matrices; any change to the
+ * group's objects or matrices (or a compute of the dpcull tree whose world matrices it is
+ * bound to) makes them stale, and a group bound to other device matrices is never cached.
+ * Results are identical either way.  Applies to culls issued and plans created after the
+ * call. */
+int dpcull_ctx_set_box_cache(dpcull_ctx ctx, int enabled);
 
 /* ---- groups: a GroupBitSet's objects and matrices resident in HBM -------------------
  * Replaces Manager::groupCreate (dp/culling/Manager.h:119). */

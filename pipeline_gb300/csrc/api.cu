@@ -72,6 +72,20 @@ struct Group {
   uint64_t incarnation = 0;
   std::vector<uint32_t> results;
   float* box_scratch = nullptr;     // partials + counter + output
+  // Box cache (see CullScene::box): prefilter boxes (kBoxRows x cap floats) and OBBs
+  // (cap x kObbFloats), allocated with the rows, and the state word.  A group whose matrices
+  // are device memory the library neither owns nor sees change (cache_volatile) is never
+  // cached; one bound to a tree of this context goes stale at every compute of that tree.
+  float* cache = nullptr;
+  float* obb = nullptr;
+  uint32_t* cache_state = nullptr;
+  bool cache_volatile = false;
+  int tree = -1;
+  // Host record of the cache, which picks the kernel: launches since it went stale, and
+  // whether a Fill launch has stored it since.  The cached kernel is only launched when
+  // `filled`; the kernels themselves read the device state word.
+  uint32_t cache_launches = 0;
+  bool cache_filled = false;
 };
 
 struct Result {
@@ -119,7 +133,7 @@ struct Plan {
   CullScene* d_scenes = nullptr;
   CullView* d_views = nullptr;
   CullView* h_views[2] = {nullptr, nullptr};   // pinned, double buffered
-  cudaGraphExec_t exec[2] = {nullptr, nullptr};
+  cudaGraphExec_t exec[3][2] = {};        // per kernel (CacheMode) and view slot, captured on first use
   cudaEvent_t done[2] = {nullptr, nullptr};
   cudaEvent_t kt[2][2] = {{nullptr, nullptr}, {nullptr, nullptr}};  // cull kernel begin / end
   bool pending[2] = {false, false};
@@ -161,6 +175,7 @@ struct dpcull_ctx_s {
   uint64_t launches = 0;
   uint64_t device_bytes = 0;
   bool exact_only = false;            // prefilter disabled (testing / ablation)
+  bool box_cache = true;              // groups keep their boxes between culls
   // Upload staging for scatter updates: pinned host and device buffers, grown on demand.
   unsigned char* stage_h = nullptr;
   unsigned char* stage_d = nullptr;
@@ -222,6 +237,17 @@ Plan* get_plan(dpcull_ctx c, dpcull_plan p)
 }
 
 size_t soa_bytes(size_t cap) { return 7 * cap * sizeof(float); }
+size_t cache_bytes(size_t cap) { return (size_t)(kBoxRows + kObbFloats) * cap * sizeof(float); }
+
+// The group's objects or matrices changed: its cached boxes are stale (in stream order, so
+// launches already queued still read the old state).
+int cache_stale(dpcull_ctx c, Group& g)
+{
+  g.cache_launches = 0;
+  g.cache_filled = false;
+  if (g.cache_state) CU(cudaMemsetAsync(g.cache_state, 0, sizeof(uint32_t), c->stream));
+  return DPCULL_OK;
+}
 
 // Grows the SoA block to hold n objects (copying the existing rows).
 int group_reserve(dpcull_ctx c, Group& g, size_t n)
@@ -233,6 +259,12 @@ int group_reserve(dpcull_ctx c, Group& g, size_t n)
   int rc = dalloc(c, (void**)&soa, soa_bytes(cap));
   if (rc) return rc;
   CU(cudaMemsetAsync(soa, 0, soa_bytes(cap), c->stream));
+  float* cache = nullptr;
+  rc = dalloc(c, (void**)&cache, cache_bytes(cap));
+  if (rc) {
+    dfree(c, soa, soa_bytes(cap));
+    return rc;
+  }
   if (g.soa && g.n)
     for (int r = 0; r < 7; ++r)
       CU(cudaMemcpyAsync(soa + (size_t)r * cap, g.soa + (size_t)r * g.cap, g.n * sizeof(float),
@@ -240,10 +272,13 @@ int group_reserve(dpcull_ctx c, Group& g, size_t n)
   if (g.soa) {
     CU(cudaStreamSynchronize(c->stream));
     dfree(c, g.soa, soa_bytes(g.cap));
+    dfree(c, g.cache, cache_bytes(g.cap));
   }
   g.soa = soa;
+  g.cache = cache;
+  g.obb = cache + (size_t)kBoxRows * cap;  // 64-byte aligned: cap is a multiple of 128
   g.cap = cap;
-  return DPCULL_OK;
+  return cache_stale(c, g);
 }
 
 // Uploads k planar objects into rows starting at object `at` (contiguous).
@@ -352,6 +387,9 @@ CullScene scene_of(Group& g, uint32_t view_begin, uint32_t n_views, uint32_t vpp
   CullScene s{};
   s.soa = g.soa;
   s.mats = g.mats;
+  s.box = g.cache_volatile ? nullptr : g.cache;  // the launch builder may still drop it
+  s.obb = g.obb;
+  s.box_state = g.cache_state;
   s.cap = (uint32_t)g.cap;
   s.n_objects = (uint32_t)g.n;
   s.n_mats = (uint32_t)std::min<size_t>(g.n_mats, 0xFFFFFFFFu);
@@ -510,6 +548,13 @@ int build_batch(dpcull_ctx c, const dpcull_job* jobs, size_t n_jobs, uint32_t vp
     scenes.push_back(s);
     if (groups_out) groups_out->push_back(jobs[j].group);
   }
+  // A cache is stored by one scene of a launch, so a group in several jobs of one launch
+  // is culled without it (as is every group with the cache switched off or the prefilter
+  // disabled).
+  std::map<const uint32_t*, int> uses;
+  for (const CullScene& sc : scenes) uses[sc.box_state]++;
+  for (CullScene& sc : scenes)
+    if (uses[sc.box_state] > 1 || c->exact_only || !c->box_cache) sc.box = nullptr;
   uint64_t tile_groups = 0;
   for (auto& s : scenes) tile_groups += (uint64_t)s.n_tiles * s.n_vgroups;
   const uint32_t it = item_tiles_for(tile_groups, c->sm_count);
@@ -535,6 +580,35 @@ int persistent_grid(dpcull_ctx c, uint32_t vpp, uint32_t ctas_per_sm, uint32_t n
 
 uint32_t max_words_of(const std::vector<CullScene>& scenes);
 
+// The kernel for a launch over these scenes (groups[i] is scene i's group): the cached one
+// when every scene's cache has been stored since it last went stale, the Fill one when
+// every scene has been culled since (so a group whose objects or matrices change every
+// frame is never stored), the fused one otherwise -- and whenever some scene has no cache.
+CacheMode batch_mode(dpcull_ctx c, const std::vector<uint32_t>& groups, const std::vector<CullScene>& scenes)
+{
+  if (scenes.empty()) return kCacheNone;
+  bool all_filled = true, all_culled = true;
+  for (size_t i = 0; i < scenes.size(); ++i) {
+    if (!scenes[i].box) return kCacheNone;
+    const Group& g = c->groups[groups[i]];
+    all_filled &= g.cache_filled;
+    all_culled &= g.cache_launches > 0;
+  }
+  return all_filled ? kCacheRead : all_culled ? kCacheFill : kCacheNone;
+}
+
+// Records a launch in the host record of every cached group it culled.
+void note_launch(dpcull_ctx c, const std::vector<uint32_t>& groups, const std::vector<CullScene>& scenes,
+                 CacheMode mode)
+{
+  for (size_t i = 0; i < scenes.size(); ++i)
+    if (scenes[i].box) {
+      Group& g = c->groups[groups[i]];
+      g.cache_launches++;
+      if (mode == kCacheFill) g.cache_filled = true;
+    }
+}
+
 // The cull over all scenes and views, then the changed-list assembly of every view.
 // d_scenes is the device copy of `scenes`.  k0 / k1 (optional, timing events) are recorded
 // right before and after the cull kernel; inside a stream capture they become
@@ -542,7 +616,7 @@ uint32_t max_words_of(const std::vector<CullScene>& scenes);
 int launch_batch(dpcull_ctx c, const CullScene* d_scenes, const CullView* d_views,
                  const std::vector<CullScene>& scenes, uint32_t n_views, uint32_t n_items,
                  uint32_t item_tiles, const dpcull_tuning& t, cudaStream_t s,
-                 cudaEvent_t k0 = nullptr, cudaEvent_t k1 = nullptr)
+                 cudaEvent_t k0 = nullptr, cudaEvent_t k1 = nullptr, CacheMode mode = kCacheNone)
 {
   if (n_views > 65535) return fail(DPCULL_ERR_INVALID_ARGUMENT, "at most 65535 views per launch");
   const uint32_t max_words = max_words_of(scenes);
@@ -557,6 +631,7 @@ int launch_batch(dpcull_ctx c, const CullScene* d_scenes, const CullView* d_view
   a.item_tiles = item_tiles;
   a.items_per_ticket = std::max<uint32_t>(1, t.tiles_per_ticket);
   a.exact_only = c->exact_only ? 1u : 0u;
+  a.cache_mode = mode;
   a.ctl = c->ctl;
   const int grid = persistent_grid(c, t.views_per_pass, t.ctas_per_sm, n_items, a.items_per_ticket);
   if (k0) CU(cudaEventRecordWithFlags(k0, s, cudaEventRecordExternal));
@@ -728,6 +803,13 @@ int dpcull_ctx_set_prefilter(dpcull_ctx c, int enabled)
   return DPCULL_OK;
 }
 
+int dpcull_ctx_set_box_cache(dpcull_ctx c, int enabled)
+{
+  if (!c) return fail(DPCULL_ERR_INVALID_ARGUMENT, "null context");
+  c->box_cache = enabled != 0;
+  return DPCULL_OK;
+}
+
 // ---- groups ------------------------------------------------------------------------
 int dpcull_group_create(dpcull_ctx c, dpcull_group* out)
 {
@@ -741,6 +823,13 @@ int dpcull_group_create(dpcull_ctx c, dpcull_group* out)
     return rc;
   }
   CU(cudaMemsetAsync(g.box_scratch, 0, (bbox_partials_needed(0) + 16) * sizeof(float), c->stream));
+  rc = dalloc(c, (void**)&g.cache_state, 16);
+  if (rc) {
+    dfree(c, g.box_scratch, (bbox_partials_needed(0) + 16) * sizeof(float));
+    g = Group();
+    return rc;
+  }
+  CU(cudaMemsetAsync(g.cache_state, 0, 16, c->stream));
   *out = (dpcull_group)(c->groups.size() - 1);
   return DPCULL_OK;
 }
@@ -753,6 +842,8 @@ int dpcull_group_destroy(dpcull_ctx c, dpcull_group gh)
   for (uint32_t r : g->results)
     if (get_result(c, r)) dpcull_result_destroy(c, r);
   dfree(c, g->soa, soa_bytes(g->cap));
+  dfree(c, g->cache, cache_bytes(g->cap));
+  dfree(c, g->cache_state, 16);
   if (g->mats_cap) dfree(c, g->mats, g->mats_cap * 64);
   dfree(c, g->box_scratch, (bbox_partials_needed(0) + 16) * sizeof(float));
   *g = Group();
@@ -778,6 +869,8 @@ int dpcull_group_set_objects(dpcull_ctx c, dpcull_group gh, size_t n, const floa
   g->max_dirty = true;
   g->n = n;
   g->incarnation += n ? n : 1;  // clearObjects + addObject x n
+  rc = cache_stale(c, *g);
+  if (rc) return rc;
   CU(cudaStreamSynchronize(c->stream));
   return DPCULL_OK;
 }
@@ -798,6 +891,8 @@ int dpcull_group_append_objects(dpcull_ctx c, dpcull_group gh, size_t k, const f
   for (size_t i = 0; i < k; ++i) g->max_xform = std::max(g->max_xform, xform[i]);
   g->n += k;
   g->incarnation += k;
+  rc = cache_stale(c, *g);
+  if (rc) return rc;
   CU(cudaStreamSynchronize(c->stream));
   return DPCULL_OK;
 }
@@ -828,7 +923,7 @@ int dpcull_group_update_objects(dpcull_ctx c, dpcull_group gh, size_t k, const u
   c->launches++;
   for (size_t i = 0; i < k; ++i) g->xform[index[i]] = xform[i];
   g->max_dirty = true;
-  return DPCULL_OK;
+  return cache_stale(c, *g);
 }
 
 int dpcull_group_remove_object(dpcull_ctx c, dpcull_group gh, size_t index)
@@ -857,7 +952,7 @@ int dpcull_group_remove_object(dpcull_ctx c, dpcull_group gh, size_t index)
     c->launches++;
   }
   g->incarnation++;
-  return DPCULL_OK;
+  return cache_stale(c, *g);
 }
 
 int dpcull_group_count(dpcull_ctx c, dpcull_group gh, size_t* n)
@@ -899,6 +994,10 @@ int dpcull_group_set_matrices(dpcull_ctx c, dpcull_group gh, const void* matrice
     }
   }
   g->n_mats = count;
+  g->cache_volatile = false;
+  g->tree = -1;
+  rc = cache_stale(c, *g);
+  if (rc) return rc;
   CU(cudaStreamSynchronize(c->stream));
   return DPCULL_OK;
 }
@@ -925,7 +1024,7 @@ int dpcull_group_update_matrices(dpcull_ctx c, dpcull_group gh, size_t k, const 
                               (uint32_t)k, nullptr, c->stream))
     return cuda_fail(cudaGetLastError(), "update matrices");
   c->launches++;
-  return DPCULL_OK;
+  return cache_stale(c, *g);
 }
 
 int dpcull_group_bind_device_matrices(dpcull_ctx c, dpcull_group gh, const float* dev, size_t count)
@@ -938,7 +1037,13 @@ int dpcull_group_bind_device_matrices(dpcull_ctx c, dpcull_group gh, const float
   g->mats = const_cast<float*>(dev);
   g->mats_cap = 0;
   g->n_mats = count;
-  return DPCULL_OK;
+  // The world matrices of a tree of this context go stale at each compute of that tree;
+  // any other device memory may change without the library seeing it: never cached.
+  g->tree = -1;
+  for (size_t t = 0; t < c->trees.size(); ++t)
+    if (c->trees[t].alive && c->trees[t].world == dev) g->tree = (int)t;
+  g->cache_volatile = g->tree < 0;
+  return cache_stale(c, *g);
 }
 
 int dpcull_group_bounding_box(dpcull_ctx c, dpcull_group gh, float lower[3], float upper[3])
@@ -1033,6 +1138,11 @@ int dpcull_cull(dpcull_ctx c, dpcull_group gh, dpcull_result rh, const float vp[
   a.exact_only = c->exact_only ? 1u : 0u;
   a.ctl = c->ctl;
   a.one_scene = scene_of(*g, 0, 1, 1, 0);
+  if (c->exact_only || !c->box_cache) a.one_scene.box = nullptr;
+  const std::vector<uint32_t> groups{gh};
+  const std::vector<CullScene> scenes{a.one_scene};
+  const CacheMode mode = batch_mode(c, groups, scenes);
+  a.cache_mode = mode;
   a.one_view = view_of(*r, vp);
   a.item_tiles = item_tiles_for(a.one_scene.n_tiles, c->sm_count);
   a.n_items = items_of(a.one_scene.n_tiles, 1, a.item_tiles);
@@ -1041,6 +1151,7 @@ int dpcull_cull(dpcull_ctx c, dpcull_group gh, dpcull_result rh, const float vp[
   if (launch_changed_lists(nullptr, a.one_view, 1, a.one_view.n_words, c->stream))
     return cuda_fail(cudaGetLastError(), "changed-list launch");
   c->launches += 3;
+  note_launch(c, groups, scenes, mode);
   return DPCULL_OK;
 }
 
@@ -1156,7 +1267,8 @@ int dpcull_cull_batched(dpcull_ctx c, const dpcull_job* jobs, size_t n_jobs, con
   std::vector<CullScene> scenes;
   std::vector<CullView> views;
   uint32_t items = 0, item_tiles = kItemTiles;
-  int rc = build_batch(c, jobs, n_jobs, t.views_per_pass, scenes, views, &items, nullptr, nullptr, &item_tiles);
+  std::vector<uint32_t> groups;
+  int rc = build_batch(c, jobs, n_jobs, t.views_per_pass, scenes, views, &items, &groups, nullptr, &item_tiles);
   if (rc) return rc;
   if (!items) return DPCULL_OK;
   CullScene* ds = nullptr;
@@ -1170,14 +1282,17 @@ int dpcull_cull_batched(dpcull_ctx c, const dpcull_job* jobs, size_t n_jobs, con
   }
   cudaMemcpyAsync(ds, scenes.data(), scenes.size() * sizeof(CullScene), cudaMemcpyHostToDevice, c->stream);
   cudaMemcpyAsync(dv, views.data(), views.size() * sizeof(CullView), cudaMemcpyHostToDevice, c->stream);
-  rc = launch_batch(c, ds, dv, scenes, (uint32_t)views.size(), items, item_tiles, t, c->stream);
+  const CacheMode mode = batch_mode(c, groups, scenes);
+  rc = launch_batch(c, ds, dv, scenes, (uint32_t)views.size(), items, item_tiles, t, c->stream, nullptr, nullptr,
+                    mode);
+  if (!rc) note_launch(c, groups, scenes, mode);
   cudaStreamSynchronize(c->stream);
   dfree(c, ds, scenes.size() * sizeof(CullScene));
   dfree(c, dv, views.size() * sizeof(CullView));
   return rc;
 }
 
-static int plan_capture(dpcull_ctx c, Plan& p, int slot)
+static int plan_capture(dpcull_ctx c, Plan& p, int slot, CacheMode mode)
 {
   cudaStream_t cs;
   CU(cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking));
@@ -1190,12 +1305,12 @@ static int plan_capture(dpcull_ctx c, Plan& p, int slot)
   if (e == cudaSuccess) {
     const uint64_t before = c->launches;
     rc = launch_batch(c, p.d_scenes, p.d_views, p.scenes, (uint32_t)p.views.size(), p.n_items,
-                      p.item_tiles, p.tuning, cs, p.kt[slot][0], p.kt[slot][1]);
+                      p.item_tiles, p.tuning, cs, p.kt[slot][0], p.kt[slot][1], mode);
     c->launches = before;  // counted when the graph is replayed
   }
   cudaError_t e2 = cudaStreamEndCapture(cs, &graph);
   if (e == cudaSuccess) e = e2;
-  if (e == cudaSuccess && rc == DPCULL_OK) e = cudaGraphInstantiate(&p.exec[slot], graph, 0);
+  if (e == cudaSuccess && rc == DPCULL_OK) e = cudaGraphInstantiate(&p.exec[mode][slot], graph, 0);
   if (graph) cudaGraphDestroy(graph);
   cudaStreamDestroy(cs);
   if (rc) return rc;
@@ -1340,7 +1455,7 @@ int dpcull_plan_create(dpcull_ctx c, const dpcull_job* jobs, size_t n_jobs,
     CU(cudaEventCreateWithFlags(&p.done[s], cudaEventDisableTiming));
     CU(cudaEventCreate(&p.kt[s][0]));
     CU(cudaEventCreate(&p.kt[s][1]));
-    rc = plan_capture(c, p, s);
+    rc = plan_capture(c, p, s, kCacheNone);  // the cache kernels' graphs on first use
     if (rc) return rc;
   }
   CU(cudaStreamSynchronize(c->stream));
@@ -1391,8 +1506,14 @@ int dpcull_plan_launch(dpcull_ctx c, dpcull_plan ph)
     for (size_t v = 0; v < p->views.size(); ++v) memcpy(p->h_views[s][v].vp, p->views[v].vp, 64);
   }
   p->fresh[s] = false;
-  CU(cudaGraphLaunch(p->exec[s], c->stream));
+  const CacheMode mode = batch_mode(c, p->groups, p->scenes);
+  if (!p->exec[mode][s]) {
+    int rc = plan_capture(c, *p, s, mode);
+    if (rc) return rc;
+  }
+  CU(cudaGraphLaunch(p->exec[mode][s], c->stream));
   CU(cudaEventRecord(p->done[s], c->stream));
+  note_launch(c, p->groups, p->scenes, mode);
   p->pending[s] = true;
   p->next ^= 1;
   c->launches += 3;  // the graph's kernels: cull, chunk counts, changed-list emission
@@ -1600,7 +1721,8 @@ int dpcull_plan_destroy(dpcull_ctx c, dpcull_plan ph)
   cudaStreamSynchronize(c->stream);
   if (p->copy_stream) cudaStreamSynchronize(p->copy_stream);  // copies into h_counts / snap
   for (int s = 0; s < 2; ++s) {
-    if (p->exec[s]) cudaGraphExecDestroy(p->exec[s]);
+    for (int m = 0; m < 3; ++m)
+      if (p->exec[m][s]) cudaGraphExecDestroy(p->exec[m][s]);
     if (p->done[s]) cudaEventDestroy(p->done[s]);
     if (p->kt[s][0]) cudaEventDestroy(p->kt[s][0]);
     if (p->kt[s][1]) cudaEventDestroy(p->kt[s][1]);
@@ -1648,10 +1770,34 @@ int dpcull_tree_create(dpcull_ctx c, size_t capacity, dpcull_tree* out)
   return DPCULL_OK;
 }
 
+// The groups that cull against a tree's world matrices: their cached boxes are stale
+// once the tree has written new world matrices.
+static int tree_groups_stale(dpcull_ctx c, dpcull_tree th)
+{
+  for (Group& g : c->groups)
+    if (g.alive && g.tree == (int)th) {
+      int rc = cache_stale(c, g);
+      if (rc) return rc;
+    }
+  return DPCULL_OK;
+}
+
+// A tree's world array is about to go away (destroy, resize): the groups bound to it no
+// longer follow the tree and are not cached until they get new matrices.
+static void tree_unbind_groups(dpcull_ctx c, dpcull_tree th)
+{
+  for (Group& g : c->groups)
+    if (g.alive && g.tree == (int)th) {
+      g.tree = -1;
+      g.cache_volatile = true;
+    }
+}
+
 int dpcull_tree_destroy(dpcull_ctx c, dpcull_tree th)
 {
   Tree* t = get_tree(c, th);
   if (!t) return fail(DPCULL_ERR_INVALID_ARGUMENT, "bad tree %u", th);
+  tree_unbind_groups(c, th);
   cudaStreamSynchronize(c->stream);
   dfree(c, t->local, t->cap * 64);
   dfree(c, t->world, t->cap * 64);
@@ -1691,6 +1837,7 @@ int dpcull_tree_resize(dpcull_ctx c, dpcull_tree th, size_t capacity)
   CU(cudaMemcpyAsync(dl, t->dirty_local, t->words * 4, cudaMemcpyDeviceToDevice, c->stream));
   CU(cudaMemcpyAsync(dw, t->dirty_world, t->words * 4, cudaMemcpyDeviceToDevice, c->stream));
   CU(cudaStreamSynchronize(c->stream));
+  tree_unbind_groups(c, th);
   dfree(c, t->local, t->cap * 64);
   dfree(c, t->world, t->cap * 64);
   dfree(c, t->dirty_local, t->words * 4);
@@ -1810,7 +1957,8 @@ int dpcull_tree_set_worlds(dpcull_ctx c, dpcull_tree th, size_t k, const uint32_
   if (!t) return fail(DPCULL_ERR_INVALID_ARGUMENT, "bad tree %u", th);
   if (!k) return DPCULL_OK;
   if (!index || !m) return fail(DPCULL_ERR_INVALID_ARGUMENT, "null arrays");
-  return tree_scatter(c, t, t->world, k, index, m, nullptr);
+  int rc = tree_scatter(c, t, t->world, k, index, m, nullptr);
+  return rc ? rc : tree_groups_stale(c, th);
 }
 
 int dpcull_tree_compute(dpcull_ctx c, dpcull_tree th)
@@ -1826,7 +1974,7 @@ int dpcull_tree_compute(dpcull_ctx c, dpcull_tree th)
     c->launches++;
   }
   CU(cudaMemsetAsync(t->dirty_local, 0, t->words * 4, c->stream));
-  return DPCULL_OK;
+  return tree_groups_stale(c, th);
 }
 
 int dpcull_tree_world_device(dpcull_ctx c, dpcull_tree th, const float** world, size_t* count)

@@ -108,12 +108,42 @@ __device__ __forceinline__ bool exact_visible(const CullScene& sc, uint32_t i, c
   const float* soa = sc.soa;
   const size_t cap = sc.cap;
   const uint32_t mi = __ldg(reinterpret_cast<const uint32_t*>(soa) + 6 * cap + i);
+  if (mi >= sc.n_mats) return false;  // reported by the host before any launch
   const float4* M = reinterpret_cast<const float4*>(sc.mats) + 4 * (size_t)mi;
   const Obb o = make_obb(__ldg(soa + i), __ldg(soa + cap + i), __ldg(soa + 2 * cap + i),
                          __ldg(soa + 3 * cap + i), __ldg(soa + 4 * cap + i),
                          __ldg(soa + 5 * cap + i), __ldg(M + 0), __ldg(M + 1), __ldg(M + 2),
                          __ldg(M + 3));
   return obb_visible(o, vp);
+}
+
+// The same test from the group's cached OBB of object i (the values make_obb computes, in
+// one 64-byte record): two 256-bit loads replace the seven scattered row reloads and the
+// matrix gather.
+__device__ __forceinline__ bool exact_visible_cached(const CullScene& sc, uint32_t i, const float* vp)
+{
+  const float* rec = sc.obb + (size_t)kObbFloats * i;
+  Obb o;
+  asm("ld.global.nc.v8.f32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
+      : "=f"(o.p.x), "=f"(o.p.y), "=f"(o.p.z), "=f"(o.p.w), "=f"(o.ex.x), "=f"(o.ex.y), "=f"(o.ex.z), "=f"(o.ex.w)
+      : "l"(rec));
+  asm("ld.global.nc.v8.f32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
+      : "=f"(o.ey.x), "=f"(o.ey.y), "=f"(o.ey.z), "=f"(o.ey.w), "=f"(o.ez.x), "=f"(o.ez.y), "=f"(o.ez.z), "=f"(o.ez.w)
+      : "l"(rec + 8));
+  return obb_visible(o, vp);
+}
+
+// Stores the reference's cached OBB of object i (Fill launches): 64 bytes, two 256-bit
+// stores.
+__device__ __forceinline__ void store_obb(const CullScene& sc, uint32_t i, const Obb& o)
+{
+  float* rec = sc.obb + (size_t)kObbFloats * i;
+  asm volatile("st.global.v8.f32 [%0], {%1,%2,%3,%4,%5,%6,%7,%8};" ::"l"(rec), "f"(o.p.x), "f"(o.p.y), "f"(o.p.z),
+               "f"(o.p.w), "f"(o.ex.x), "f"(o.ex.y), "f"(o.ex.z), "f"(o.ex.w)
+               : "memory");
+  asm volatile("st.global.v8.f32 [%0], {%1,%2,%3,%4,%5,%6,%7,%8};" ::"l"(rec + 8), "f"(o.ey.x), "f"(o.ey.y), "f"(o.ey.z),
+               "f"(o.ey.w), "f"(o.ez.x), "f"(o.ez.y), "f"(o.ez.z), "f"(o.ez.w)
+               : "memory");
 }
 
 // The lane's 4 visibility bits of one view (bit k = object k) into the tile's words of
@@ -246,7 +276,8 @@ __device__ __forceinline__ uint32_t warp_scan(uint32_t x, int lane)
 }
 
 // Runs the queued undecided pairs through the exact test, all lanes together, and sets
-// the visible ones in the item's words.
+// the visible ones in the item's words.  OBBS: the group's OBB cache is valid.
+template <bool OBBS>
 __device__ __forceinline__ void drain_queue(WarpShared& ws, const CullScene& sc, uint32_t tile_first,
                                             uint32_t qn, int lane)
 {
@@ -254,24 +285,113 @@ __device__ __forceinline__ void drain_queue(WarpShared& ws, const CullScene& sc,
   for (uint32_t q = lane; q < qn; q += 32) {
     const uint32_t e = ws.queue[q];
     const uint32_t t = e >> 10, o = (e >> 3) & 127u, v = e & 7u;
-    if (exact_visible(sc, (tile_first + t) * kTileObjects + o, ws.cv[v].vp))
+    const uint32_t i = (tile_first + t) * kTileObjects + o;
+    if (OBBS ? exact_visible_cached(sc, i, ws.cv[v].vp) : exact_visible(sc, i, ws.cv[v].vp))
       atomicOr(&ws.words[v][t][o >> 5], 1u << (o & 31));
   }
   __syncwarp();
 }
 
+template <uint32_t MODE>
+__device__ __forceinline__ void drain(WarpShared& ws, const CullScene& sc, uint32_t tile_first, uint32_t qn,
+                                      int lane, bool obbs)
+{
+  if (MODE == kCacheRead && obbs) drain_queue<true>(ws, sc, tile_first, qn, lane);
+  else drain_queue<false>(ws, sc, tile_first, qn, lane);
+}
+
+// The lane's undecided pairs of tile t into the warp's queue (drained early only if it
+// would overflow).  Returns the new queue length.
+template <int VPP, uint32_t MODE>
+__device__ __forceinline__ uint32_t push_undecided(WarpShared& ws, const CullScene& sc, uint32_t tile_first,
+                                                   uint32_t t, uint32_t qn, uint32_t amb, int lane, bool obbs)
+{
+  const uint32_t cnt = (uint32_t)__popc(amb);
+  const uint32_t incl = warp_scan(cnt, lane);
+  const uint32_t tot = __shfl_sync(0xffffffffu, incl, 31);
+  if (tot) {  // uniform over the warp
+    if (qn + tot > (uint32_t)kQueueCap) {
+      drain<MODE>(ws, sc, tile_first, qn, lane, obbs);
+      qn = 0;
+    }
+    uint32_t pos = qn + incl - cnt;
+    while (amb) {
+      const int b = __ffs(amb) - 1;
+      ws.queue[pos++] = (uint16_t)((t << 10) | (((uint32_t)lane * kObjPerThread + und_object<VPP>(b)) << 3) |
+                                   und_view<VPP>(b));
+      amb &= amb - 1u;
+    }
+    qn += tot;
+  }
+  return qn;
+}
+
+// The lane's 4 prefilter boxes of a tile from the group's box cache.  The Fill launch that
+// validated it found every transform index in range, so only the object count limits which
+// boxes are used.
+__device__ __forceinline__ uint32_t cached_boxes(const CullScene& sc, uint32_t obj0, pf::Box (&bx)[kObjPerThread])
+{
+  const size_t cap = sc.cap;
+  const float4 cx = ld_stream4(sc.box + 0 * cap + obj0), cy = ld_stream4(sc.box + 1 * cap + obj0);
+  const float4 cz = ld_stream4(sc.box + 2 * cap + obj0), r = ld_stream4(sc.box + 3 * cap + obj0);
+  const float4 d0 = ld_stream4(sc.box + 4 * cap + obj0);
+  uint32_t valid = 0;
+#pragma unroll
+  for (int k = 0; k < kObjPerThread; ++k) {
+    bx[k] = pf::Box{comp(cx, k), comp(cy, k), comp(cz, k), comp(r, k), comp(d0, k)};
+    valid |= (uint32_t)(obj0 + k < sc.n_objects) << k;
+  }
+  return valid;
+}
+
+// Stores the lane's 4 prefilter boxes into the group's box cache (Fill launches).
+__device__ __forceinline__ void store_boxes(const CullScene& sc, uint32_t obj0, const pf::Box (&bx)[kObjPerThread])
+{
+  const size_t cap = sc.cap;
+  __stcg(reinterpret_cast<float4*>(sc.box + 0 * cap + obj0), make_float4(bx[0].cx, bx[1].cx, bx[2].cx, bx[3].cx));
+  __stcg(reinterpret_cast<float4*>(sc.box + 1 * cap + obj0), make_float4(bx[0].cy, bx[1].cy, bx[2].cy, bx[3].cy));
+  __stcg(reinterpret_cast<float4*>(sc.box + 2 * cap + obj0), make_float4(bx[0].cz, bx[1].cz, bx[2].cz, bx[3].cz));
+  __stcg(reinterpret_cast<float4*>(sc.box + 3 * cap + obj0), make_float4(bx[0].r, bx[1].r, bx[2].r, bx[3].r));
+  __stcg(reinterpret_cast<float4*>(sc.box + 4 * cap + obj0), make_float4(bx[0].d0, bx[1].d0, bx[2].d0, bx[3].d0));
+}
+
 // Classification of one tile into the item's words (visible objects) and queue
 // (undecided pairs).  Returns the new queue length.  WIDE: the scene's matrix array is
-// 32-byte aligned (two 256-bit loads per matrix).
-template <int VPP, bool PF, bool WIDE>
+// 32-byte aligned (two 256-bit loads per matrix).  MODE: the fused kernel computes the
+// boxes from the rows and the world matrices, the Fill kernel also stores them (and the
+// OBBs), the cached kernel reads them (cache_ok: the scene's cache is valid; if not, every
+// pair of the tile goes to the exact test).
+template <int VPP, bool PF, bool WIDE, uint32_t MODE>
 __device__ __forceinline__ uint32_t classify_tile(const CullLaunch& a, WarpShared& ws, const CullScene& sc,
                                                   uint32_t tile, uint32_t t, uint32_t tile_first,
-                                                  uint32_t n_t, int nv, uint32_t qn, int lane,
+                                                  uint32_t n_t, int nv, uint32_t qn, int lane, bool cache_ok,
                                                   const uint4 xf_cur, uint4& xf_next)
 {
   const uint32_t obj0 = tile * kTileObjects + (uint32_t)lane * kObjPerThread;
   const float* soa = sc.soa;
   const size_t cap = sc.cap;
+  if (PF && MODE == kCacheRead) {
+    pf::Box bx[kObjPerThread];
+    uint32_t amb;
+    if (cache_ok) {
+      const uint32_t valid = cached_boxes(sc, obj0, bx);
+      amb = classify_views<VPP>(ws, bx, nv, t, valid, lane);
+    } else {
+      // A Stale cache (the host never launches this kernel on one): no visible bit from the
+      // prefilter, every pair of the lane's objects to the exact test.
+      uint32_t valid = 0;
+#pragma unroll
+      for (int k = 0; k < kObjPerThread; ++k) valid |= (uint32_t)(obj0 + k < sc.n_objects) << k;
+      if (VPP == 1) {
+        amb = (valid * 0x204081u) & 0x01010101u;
+        store_nibble(ws, 0, t, 0u, lane);
+      } else {
+        amb = (valid * 0x11111111u) & (nv >= 8 ? 0xFFFFFFFFu : (1u << (4 * nv)) - 1u);
+        if ((lane & 7) < nv) ws.words[lane & 7][t][lane >> 3] = 0u;
+      }
+    }
+    return push_undecided<VPP, MODE>(ws, sc, tile_first, t, qn, amb, lane, cache_ok);
+  }
   // The transform indices of this tile were loaded one tile ahead, so the matrix gathers
   // below go out together with the other rows; the next tile's indices go out now.
   const uint4 xf = xf_cur;
@@ -282,7 +402,6 @@ __device__ __forceinline__ uint32_t classify_tile(const CullLaunch& a, WarpShare
   const float4 ex = ld_stream4(soa + 3 * cap + obj0);
   const float4 ey = ld_stream4(soa + 4 * cap + obj0);
   const float4 ez = ld_stream4(soa + 5 * cap + obj0);
-  uint32_t amb = 0;
   if (PF) {
     // Prefilter boxes of the 4 objects first (their matrix gathers overlap), then each
     // view's planes are read once for all 4 objects.
@@ -304,60 +423,43 @@ __device__ __forceinline__ uint32_t classify_tile(const CullLaunch& a, WarpShare
       const pf::F4 m2{r2.x, r2.y, r2.z, r2.w}, m3{r3.x, r3.y, r3.z, r3.w};
       bx[k] = pf::make_box(comp(lx, k), comp(ly, k), comp(lz, k), comp(ex, k), comp(ey, k),
                            comp(ez, k), m0, m1, m2, m3);
+      if (MODE == kCacheFill && use && sc.box)
+        store_obb(sc, obj0 + k, make_obb(comp(lx, k), comp(ly, k), comp(lz, k), comp(ex, k), comp(ey, k),
+                                         comp(ez, k), r0, r1, r2, r3));
       valid |= (uint32_t)use << k;
     }
     if (VPP > 1 && bad) {
       const uint32_t o = obj0 + (uint32_t)__ffs(bad) - 1u;
       if (atomicOr(&a.ctl->error, kErrBadTransform) == 0) a.ctl->error_info = o;
     }
-    amb = classify_views<VPP>(ws, bx, nv, t, valid, lane);
-  } else {
-    // Exact test only: every pair in the reference's operation order (the box is rebuilt
-    // per view from the loaded rows; the matrix reloads hit L1).
-    const float4* mats = reinterpret_cast<const float4*>(sc.mats);
-    uint32_t use = 0;
+    if (MODE == kCacheFill && sc.box) store_boxes(sc, obj0, bx);
+    const uint32_t amb = classify_views<VPP>(ws, bx, nv, t, valid, lane);
+    return push_undecided<VPP, MODE>(ws, sc, tile_first, t, qn, amb, lane, false);
+  }
+  // Exact test only: every pair in the reference's operation order (the box is rebuilt
+  // per view from the loaded rows; the matrix reloads hit L1).
+  const float4* mats = reinterpret_cast<const float4*>(sc.mats);
+  uint32_t use = 0;
 #pragma unroll
-    for (int k = 0; k < kObjPerThread; ++k) {
-      if (obj0 + k < sc.n_objects) {
-        if (compu(xf, k) < sc.n_mats) use |= 1u << k;
-        else if (atomicOr(&a.ctl->error, kErrBadTransform) == 0) a.ctl->error_info = obj0 + k;
-      }
-    }
-#pragma unroll 1
-    for (int v = 0; v < nv; ++v) {
-      uint32_t nib = 0;
-#pragma unroll
-      for (int k = 0; k < kObjPerThread; ++k) {
-        if (use & (1u << k)) {
-          const float4* M = mats + 4 * (size_t)compu(xf, k);
-          const Obb o = make_obb(comp(lx, k), comp(ly, k), comp(lz, k), comp(ex, k), comp(ey, k),
-                                 comp(ez, k), __ldg(M + 0), __ldg(M + 1), __ldg(M + 2), __ldg(M + 3));
-          if (obb_visible(o, ws.cv[v].vp)) nib |= 1u << k;
-        }
-      }
-      store_nibble(ws, v, t, nib, lane);
+  for (int k = 0; k < kObjPerThread; ++k) {
+    if (obj0 + k < sc.n_objects) {
+      if (compu(xf, k) < sc.n_mats) use |= 1u << k;
+      else if (atomicOr(&a.ctl->error, kErrBadTransform) == 0) a.ctl->error_info = obj0 + k;
     }
   }
-
-  // The undecided pairs into the queue (drained early only if it would overflow).
-  if (PF) {
-    const uint32_t cnt = (uint32_t)__popc(amb);
-    const uint32_t incl = warp_scan(cnt, lane);
-    const uint32_t tot = __shfl_sync(0xffffffffu, incl, 31);
-    if (tot) {  // uniform over the warp
-      if (qn + tot > (uint32_t)kQueueCap) {
-        drain_queue(ws, sc, tile_first, qn, lane);
-        qn = 0;
+#pragma unroll 1
+  for (int v = 0; v < nv; ++v) {
+    uint32_t nib = 0;
+#pragma unroll
+    for (int k = 0; k < kObjPerThread; ++k) {
+      if (use & (1u << k)) {
+        const float4* M = mats + 4 * (size_t)compu(xf, k);
+        const Obb o = make_obb(comp(lx, k), comp(ly, k), comp(lz, k), comp(ex, k), comp(ey, k),
+                               comp(ez, k), __ldg(M + 0), __ldg(M + 1), __ldg(M + 2), __ldg(M + 3));
+        if (obb_visible(o, ws.cv[v].vp)) nib |= 1u << k;
       }
-      uint32_t pos = qn + incl - cnt;
-      while (amb) {
-        const int b = __ffs(amb) - 1;
-        ws.queue[pos++] = (uint16_t)((t << 10) | (((uint32_t)lane * kObjPerThread + und_object<VPP>(b)) << 3) |
-                                     und_view<VPP>(b));
-        amb &= amb - 1u;
-      }
-      qn += tot;
     }
+    store_nibble(ws, v, t, nib, lane);
   }
   return qn;
 }
@@ -401,7 +503,7 @@ __device__ __forceinline__ void finish_item(const WarpShared& ws, uint32_t tile_
 // One work item (up to kItemTiles tiles of 128 objects x one group of up to VPP views)
 // by one warp.  ws.sc and `vkey` cache the warp's current scene and staged view group
 // across items.
-template <int VPP, bool PF, bool WIDE>
+template <int VPP, bool PF, bool WIDE, uint32_t MODE>
 __device__ __forceinline__ void warp_item(const CullLaunch& a, uint32_t item, WarpShared& ws,
                                           uint32_t& vkey)
 {
@@ -425,8 +527,13 @@ __device__ __forceinline__ void warp_item(const CullLaunch& a, uint32_t item, Wa
   const int nv = (int)min((uint32_t)VPP, sc.n_views - vfirst);
   const uint32_t tile_first = group * a.item_tiles;
   const uint32_t n_t = min(a.item_tiles, sc.n_tiles - tile_first);
-  // The first tile's transform indices load while the views are staged.
-  const uint4 xf_first = ld_stream4u(sc.soa + 6 * (size_t)sc.cap + tile_first * kTileObjects + (uint32_t)lane * kObjPerThread);
+  // The cached kernel reads the scene's cache state once per item (it does not change
+  // during a launch); the other kernels load the first tile's transform indices while the
+  // views are staged.
+  const bool cache_ok = PF && MODE == kCacheRead && sc.box && __ldcg(sc.box_state) == kBoxValid;
+  uint4 xf_first = make_uint4(0u, 0u, 0u, 0u);
+  if (!(PF && MODE == kCacheRead))
+    xf_first = ld_stream4u(sc.soa + 6 * (size_t)sc.cap + tile_first * kTileObjects + (uint32_t)lane * kObjPerThread);
 
   // Stage the views (matrices and output pointers) and their prefilter planes in the
   // warp's shared memory when the view group changes; consecutive items of one scene
@@ -463,15 +570,16 @@ __device__ __forceinline__ void warp_item(const CullLaunch& a, uint32_t item, Wa
   uint4 xf = xf_first;
   for (uint32_t t = 0; t < n_t; ++t) {
     uint4 xf_next = make_uint4(0u, 0u, 0u, 0u);
-    qn = classify_tile<VPP, PF, WIDE>(a, ws, sc, tile_first + t, t, tile_first, n_t, nv, qn, lane, xf, xf_next);
+    qn = classify_tile<VPP, PF, WIDE, MODE>(a, ws, sc, tile_first + t, t, tile_first, n_t, nv, qn, lane, cache_ok, xf,
+                                            xf_next);
     xf = xf_next;
   }
-  if (PF && qn) drain_queue(ws, sc, tile_first, qn, lane);
+  if (PF && qn) drain<MODE>(ws, sc, tile_first, qn, lane, cache_ok);
   else __syncwarp();
   finish_item<VPP>(ws, tile_first, n_t, nv, lane);
 }
 
-template <int VPP, bool PF, bool WIDE>
+template <int VPP, bool PF, bool WIDE, uint32_t MODE>
 __global__ void __launch_bounds__(kThreads, 3) cull_kernel(const __grid_constant__ CullLaunch a)
 {
   __shared__ WarpShared wsh[kThreads / 32];
@@ -493,15 +601,28 @@ __global__ void __launch_bounds__(kThreads, 3) cull_kernel(const __grid_constant
     uint32_t next = 0;
     if (lane == 0) next = atomicAdd(&ctl->ticket, a.items_per_ticket);
     const uint32_t last = min(first + a.items_per_ticket, a.n_items);
-    for (uint32_t item = first; item < last; ++item) warp_item<VPP, PF, WIDE>(a, item, ws, vkey);
+    for (uint32_t item = first; item < last; ++item) warp_item<VPP, PF, WIDE, MODE>(a, item, ws, vkey);
     first = __shfl_sync(0xffffffffu, next, 0);
   }
+  __shared__ bool last_cta;
   __syncthreads();
   if (threadIdx.x == 0) {
-    __threadfence();
-    const unsigned int prev = atomicAdd(&ctl->done, 1u);
-    if (prev == gridDim.x - 1) {
-      // Last CTA of the launch: reset the ticket for the next launch (no memset needed).
+    __threadfence();  // this CTA's stores (words, cached boxes) before its count
+    last_cta = atomicAdd(&ctl->done, 1u) == gridDim.x - 1;
+  }
+  __syncthreads();
+  if (last_cta) {
+    // Last CTA of the launch: every other CTA has finished.  A Fill launch validates the
+    // caches it stored (not after finding a bad transform index); then the ticket is reset
+    // for the next launch (no memset needed).
+    if (PF && MODE == kCacheFill && *(volatile unsigned int*)&ctl->error == 0u) {
+      const uint32_t ns = a.scenes ? a.n_scenes : 1u;
+      for (uint32_t i = threadIdx.x; i < ns; i += blockDim.x) {
+        const CullScene& sc = a.scenes ? a.scenes[i] : a.one_scene;
+        if (sc.box) *sc.box_state = kBoxValid;
+      }
+    }
+    if (threadIdx.x == 0) {
       ctl->ticket = 0;
       ctl->done = 0;
     }
@@ -604,12 +725,20 @@ __global__ void __launch_bounds__(kScanThreads)
   }
 }
 
+template <int VPP, bool WIDE>
+void launch_pf(const CullLaunch& a, int grid, cudaStream_t s)
+{
+  if (a.cache_mode == kCacheRead) cull_kernel<VPP, true, WIDE, kCacheRead><<<grid, kThreads, 0, s>>>(a);
+  else if (a.cache_mode == kCacheFill) cull_kernel<VPP, true, WIDE, kCacheFill><<<grid, kThreads, 0, s>>>(a);
+  else cull_kernel<VPP, true, WIDE, kCacheNone><<<grid, kThreads, 0, s>>>(a);
+}
+
 template <int VPP>
 int launch_vpp(const CullLaunch& a, int grid, cudaStream_t s)
 {
-  if (a.exact_only) cull_kernel<VPP, false, false><<<grid, kThreads, 0, s>>>(a);
-  else if (a.wide_mats) cull_kernel<VPP, true, true><<<grid, kThreads, 0, s>>>(a);
-  else cull_kernel<VPP, true, false><<<grid, kThreads, 0, s>>>(a);
+  if (a.exact_only) cull_kernel<VPP, false, false, kCacheNone><<<grid, kThreads, 0, s>>>(a);
+  else if (a.wide_mats) launch_pf<VPP, true>(a, grid, s);
+  else launch_pf<VPP, false>(a, grid, s);
   return cudaGetLastError() == cudaSuccess ? 0 : -1;
 }
 
@@ -617,7 +746,8 @@ template <int VPP>
 int max_ctas()
 {
   int n = 0;
-  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, cull_kernel<VPP, true, true>, kThreads, 0) != cudaSuccess)
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, cull_kernel<VPP, true, true, kCacheNone>, kThreads, 0) !=
+      cudaSuccess)
     return 1;
   return n > 0 ? n : 1;
 }

@@ -62,9 +62,30 @@ DPCULL_HD_CONST size_t chunks_of(size_t n_words) { return (n_words + kDeltaChunk
 constexpr uint32_t kErrBadTransform = 1u;   // transform index >= matrix count
 constexpr uint32_t kErrMisaligned = 2u;     // a wide launch met a matrix array not 32-byte aligned
 
+// Box cache of a group (the counterpart of the reference's OBB cache, GroupCPU::updateOBBs,
+// dp/culling/cpu/src/ManagerImpl.cpp:114-162): per object the prefilter box of
+// dpcull_prefilter.h -- centre x, y, z, radius, margin -- in 5 planar rows of `cap` floats,
+// and the reference's cached OBB (point and three axes, computed in its operation order:
+// one 64-byte record per object) for the exact test of the pairs the prefilter leaves
+// undecided.  Its state word is Valid once a Fill launch has stored the boxes of the
+// group's current objects and matrices; the host resets it to Stale (in stream order)
+// whenever they change.  Three kernels (CacheMode): the fused one computes every box from
+// the rows and the world matrices, the Fill one also stores them and validates the cache,
+// the cached one reads them -- and should it meet a group whose cache is Stale, it sends
+// all of that group's pairs to the exact test instead, so its results never depend on the
+// host's choice of kernel.
+constexpr uint32_t kBoxStale = 0u;
+constexpr uint32_t kBoxValid = 1u;
+constexpr int kBoxRows = 5;
+constexpr int kObbFloats = 16;
+enum CacheMode : uint32_t { kCacheNone = 0u, kCacheFill = 1u, kCacheRead = 2u };
+
 struct CullScene {
   const float* soa;        // base of the group's SoA block
   const float* mats;       // [n_mats][16]
+  float* box;              // prefilter-box cache [kBoxRows][cap], or nullptr (not cached)
+  float* obb;              // OBB cache [cap][kObbFloats] (present with box)
+  uint32_t* box_state;     // the caches' state word (kBoxStale / kBoxValid)
   uint32_t cap;            // SoA row stride (objects)
   uint32_t n_objects;
   uint32_t n_mats;
@@ -109,6 +130,7 @@ struct CullLaunch {
   uint32_t exact_only;       // 1 = skip the conservative prefilter (every pair exact)
   uint32_t wide_mats;        // 1 = every scene's matrix array is 32-byte aligned (256-bit
                              // matrix loads); set by launch_cull itself for `one_scene`
+  uint32_t cache_mode;       // CacheMode: the fused, Fill or cached kernel (the host's choice)
   CullControl* ctl;
   CullScene one_scene;
   CullView one_view;

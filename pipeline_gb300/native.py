@@ -58,6 +58,7 @@ _SIGS = {
     "dpcull_ctx_kernel_launches": (C.c_uint64, [_P]),
     "dpcull_ctx_device_bytes": (C.c_uint64, [_P]),
     "dpcull_ctx_set_prefilter": (_I, [_P, _I]),
+    "dpcull_ctx_set_box_cache": (_I, [_P, _I]),
     "dpcull_group_create": (_I, [_P, _UP]),
     "dpcull_group_destroy": (_I, [_P, _U32]),
     "dpcull_group_set_objects": (_I, [_P, _U32, _SZ, _FP, _FP, _UP]),
@@ -225,6 +226,10 @@ class Context:
 
     def set_prefilter(self, enabled: bool) -> None:
         _check(self.lib.dpcull_ctx_set_prefilter(self.h, 1 if enabled else 0))
+
+    def set_box_cache(self, enabled: bool) -> None:
+        """Keep (default) or recompute the groups' boxes between culls (identical results)."""
+        _check(self.lib.dpcull_ctx_set_box_cache(self.h, 1 if enabled else 0))
 
     # ---- groups ----
     def group_create(self) -> int:

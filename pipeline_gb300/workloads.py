@@ -269,13 +269,49 @@ def batched_scenes(seed: int = 2, n_scenes: int = 256, nmin: float = 1e3, nmax: 
         return list(ex.map(make, range(n_scenes)))
 
 
-def stress_scene(seed: int = 3, n_objects: int = 16_000_000, n_transforms: int = 1_000_000):
+STRESS_CHUNK = 1 << 20  # objects per independently seeded chunk of the stress scene
+
+
+def stress_scene(seed: int = 3, n_objects: int = 16_000_000, n_transforms: int = 1_000_000,
+                 begin: int = 0, end: int | None = None, workers: int | None = None):
+    """The bandwidth stress scene, or the objects [begin, end) of it (a shard).  The
+    shared world matrices come from `seed`; the objects are generated in chunks of
+    STRESS_CHUNK objects, each from its own child seed, so a shard is generated without
+    the rest of the scene (and the chunks in parallel): every rank of a multi-GPU run
+    holds exactly its part of one global scene."""
+    import concurrent.futures as cf
+    import os
+
+    end = n_objects if end is None else min(end, n_objects)
     rng = np.random.default_rng(seed)
     mats = random_matrices(rng, n_transforms)
-    lower, upper, extent = random_boxes(rng, n_objects)
-    xform = rng.integers(0, n_transforms, n_objects, dtype=np.uint32)
+    n_chunks = -(-n_objects // STRESS_CHUNK)
+    seeds = np.random.SeedSequence([seed, 1]).spawn(n_chunks)
+    n = max(end - begin, 0)
+    lower = np.empty((3, n), np.float32)
+    upper = np.empty((3, n), np.float32)
+    extent = np.empty((3, n), np.float32)
+    xform = np.empty(n, np.uint32)
+
+    def fill(c: int) -> None:
+        c0, c1 = c * STRESS_CHUNK, min(n_objects, (c + 1) * STRESS_CHUNK)
+        lo, hi = max(c0, begin), min(c1, end)
+        if lo >= hi:
+            return
+        r = np.random.default_rng(seeds[c])
+        l_, u_, e_ = random_boxes(r, c1 - c0)
+        x_ = r.integers(0, n_transforms, c1 - c0, dtype=np.uint32)
+        a, b = lo - c0, hi - c0
+        lower[:, lo - begin:hi - begin] = l_[:, a:b]
+        upper[:, lo - begin:hi - begin] = u_[:, a:b]
+        extent[:, lo - begin:hi - begin] = e_[:, a:b]
+        xform[lo - begin:hi - begin] = x_[a:b]
+
+    chunks = range(begin // STRESS_CHUNK, -(-end // STRESS_CHUNK)) if n else range(0)
+    with cf.ThreadPoolExecutor(max_workers=workers or min(16, os.cpu_count() or 1)) as ex:
+        list(ex.map(fill, chunks))
     vps = f32(cube_face_views() + stereo_views())
-    return dict(lower=lower, upper=upper, extent=extent, xform=xform, mats=mats, vps=vps)
+    return dict(lower=lower, upper=upper, extent=extent, xform=xform, mats=mats, vps=vps, first=begin)
 
 
 def jitter_view(rng: np.random.Generator, vp: np.ndarray, max_deg: float = 2.0) -> np.ndarray:
