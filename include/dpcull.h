@@ -69,6 +69,10 @@ void* dpcull_ctx_stream(dpcull_ctx ctx);
 uint64_t dpcull_ctx_kernel_launches(dpcull_ctx ctx);
 /* Device bytes currently held by the context. */
 uint64_t dpcull_ctx_device_bytes(dpcull_ctx ctx);
+/* Cull-kernel launches of this context so far, by kind: out[0] the kernel that transforms
+ * every box (no box cache), out[1] the one that also stores the box cache, out[2] the one
+ * that reads it.  Every dpcull_cull, dpcull_cull_batched and dpcull_plan_launch counts one. */
+int dpcull_ctx_cull_launches(dpcull_ctx ctx, uint64_t out[3]);
 /* Enables (default) or disables the conservative prefilter for launches made after the
  * call (plans keep the setting they were created with).  Results are identical either
  * way: the prefilter only decides object-views whose outcome is certain under the
@@ -81,8 +85,8 @@ int dpcull_ctx_set_prefilter(dpcull_ctx ctx, int enabled);
  * later cull reads them instead of the objects and their world matrices; any change to the
  * group's objects or matrices (or a compute of the dpcull tree whose world matrices it is
  * bound to) makes them stale, and a group bound to other device matrices is never cached.
- * Results are identical either way.  Applies to culls issued and plans created after the
- * call. */
+ * Results are identical either way.  Applies to every cull, batched cull and plan launch
+ * issued after the call (plans created before it included). */
 int dpcull_ctx_set_box_cache(dpcull_ctx ctx, int enabled);
 
 /* ---- groups: a GroupBitSet's objects and matrices resident in HBM -------------------

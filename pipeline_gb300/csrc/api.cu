@@ -173,6 +173,7 @@ struct dpcull_ctx_s {
   unsigned int* h_err = nullptr;     // pinned: ctl->error, error_info, one scratch word
   int sm_count = 0;
   uint64_t launches = 0;
+  uint64_t mode_launches[3] = {0, 0, 0};  // cull kernels by CacheMode
   uint64_t device_bytes = 0;
   bool exact_only = false;            // prefilter disabled (testing / ablation)
   bool box_cache = true;              // groups keep their boxes between culls
@@ -583,10 +584,12 @@ uint32_t max_words_of(const std::vector<CullScene>& scenes);
 // The kernel for a launch over these scenes (groups[i] is scene i's group): the cached one
 // when every scene's cache has been stored since it last went stale, the Fill one when
 // every scene has been culled since (so a group whose objects or matrices change every
-// frame is never stored), the fused one otherwise -- and whenever some scene has no cache.
+// frame is never stored), the fused one otherwise -- and whenever some scene has no cache
+// or the context has the cache switched off (a plan keeps the box pointers it was
+// created with, so the switch is read here, at every launch).
 CacheMode batch_mode(dpcull_ctx c, const std::vector<uint32_t>& groups, const std::vector<CullScene>& scenes)
 {
-  if (scenes.empty()) return kCacheNone;
+  if (scenes.empty() || !c->box_cache || c->exact_only) return kCacheNone;
   bool all_filled = true, all_culled = true;
   for (size_t i = 0; i < scenes.size(); ++i) {
     if (!scenes[i].box) return kCacheNone;
@@ -601,6 +604,7 @@ CacheMode batch_mode(dpcull_ctx c, const std::vector<uint32_t>& groups, const st
 void note_launch(dpcull_ctx c, const std::vector<uint32_t>& groups, const std::vector<CullScene>& scenes,
                  CacheMode mode)
 {
+  c->mode_launches[mode]++;
   for (size_t i = 0; i < scenes.size(); ++i)
     if (scenes[i].box) {
       Group& g = c->groups[groups[i]];
@@ -795,6 +799,13 @@ int dpcull_ctx_synchronize(dpcull_ctx c)
 void* dpcull_ctx_stream(dpcull_ctx c) { return c ? (void*)c->stream : nullptr; }
 uint64_t dpcull_ctx_kernel_launches(dpcull_ctx c) { return c ? c->launches : 0; }
 uint64_t dpcull_ctx_device_bytes(dpcull_ctx c) { return c ? c->device_bytes : 0; }
+
+int dpcull_ctx_cull_launches(dpcull_ctx c, uint64_t out[3])
+{
+  if (!c || !out) return fail(DPCULL_ERR_INVALID_ARGUMENT, "null context or output");
+  for (int k = 0; k < 3; ++k) out[k] = c->mode_launches[k];
+  return DPCULL_OK;
+}
 
 int dpcull_ctx_set_prefilter(dpcull_ctx c, int enabled)
 {

@@ -192,62 +192,75 @@ __device__ __forceinline__ uint32_t transpose_nibbles8(uint32_t x, int lane)
   return x;
 }
 
+// Object K of the lane's 4 in one view: its six plane values (each axis' lo and hi plane
+// as one fma.rn.f32x2 pair, the FMA chain of pf::plane) and the group decision as bit K of
+// `in` (visible) and of `un` (undecided).
+template <int K>
+__device__ __forceinline__ void decide_object(const unsigned long long (&cx)[kObjPerThread],
+                                              const unsigned long long (&cy)[kObjPerThread],
+                                              const unsigned long long (&cz)[kObjPerThread],
+                                              const ulonglong2& ax0, const ulonglong2& ax1,
+                                              const ulonglong2& ay0, const ulonglong2& ay1,
+                                              const ulonglong2& az0, const ulonglong2& az1,
+                                              const float (&D)[kObjPerThread], const float (&nT)[kObjPerThread],
+                                              uint32_t& in, uint32_t& un)
+{
+  float xl, xh, yl, yh, zl, zh;
+  upk2(fma2(cz[K], ax1.x, fma2(cy[K], ax0.y, fma2(cx[K], ax0.x, ax1.y))), xl, xh);
+  upk2(fma2(cz[K], ay1.x, fma2(cy[K], ay0.y, fma2(cx[K], ay0.x, ay1.y))), yl, yh);
+  upk2(fma2(cz[K], az1.x, fma2(cy[K], az0.y, fma2(cx[K], az0.x, az1.y))), zl, zh);
+  pf::decide_bits<1u << K>(xl, xh, yl, yh, zl, zh, D[K], nT[K], in, un);
+}
+
 // Prefilter of the lane's 4 boxes in each view of the item; returns the undecided pairs
-// (bit layout: und_object / und_view below).  With several views the visible bits collect as nibbles (bit 4v + k:
-// object k, view v) and one nibble transpose per tile gives every lane one visibility
-// word (view lane & 7, word lane >> 3 of the tile): 3 shuffles per tile instead of 3 per
-// view.  With one view the nibble goes to its word directly (the 1-view kernel keeps its
-// registers better that way).  The lo and hi planes of an axis are evaluated as one pair
-// (fma.rn.f32x2 on the pairs the view staging interleaved: 9 paired FMAs instead of 18
-// per pair of box and view, each half the same fma.rn.f32 chain as pf::plane), then
-// pf::decide_group decides against the view group's margin (each box's two thresholds
-// are computed once for all the group's views; all-ones / zero masks, so each decision
-// becomes its bit with one logic operation).  Branch-free per pair; the view loop is not
-// unrolled (nv is uniform over the warp).
+// (bit layout: und_object / und_view below).  With several views the visible bits collect
+// as nibbles (bit 4v + k: object k, view v) and one nibble transpose per tile gives every
+// lane one visibility word (view lane & 7, word lane >> 3 of the tile): 3 shuffles per tile
+// instead of 3 per view.  The views run last to first and each view's nibbles are shifted
+// in below the later views' (no per-view shift by v).  With one view the nibble goes to
+// its word directly (the 1-view kernel keeps its registers better that way).  Per pair of
+// box and view: 9 paired FMAs for the six plane values, then pf::decide_bits against the
+// view group's margin (each box's two thresholds are computed once for all the group's
+// views): one comparison and one predicated OR per bit.  Branch-free per pair; the view
+// loop is not unrolled (nv is uniform over the warp).
 template <int VPP>
 __device__ __forceinline__ uint32_t classify_views(WarpShared& ws, const pf::Box (&bx)[kObjPerThread],
                                                    int nv, uint32_t t, uint32_t valid, int lane)
 {
+  static_assert(kObjPerThread == 4, "decide_object is called for objects 0..3");
   // Per box: its centre as (c, c) pairs and its two thresholds against the group margin,
   // once for all views.
   unsigned long long cx[kObjPerThread], cy[kObjPerThread], cz[kObjPerThread];
-  float D[kObjPerThread], T[kObjPerThread];
+  float D[kObjPerThread], nT[kObjPerThread];
   const pf::GroupMargin gm = ws.gm;
 #pragma unroll
   for (int k = 0; k < kObjPerThread; ++k) {
     cx[k] = pk2(bx[k].cx, bx[k].cx);
     cy[k] = pk2(bx[k].cy, bx[k].cy);
     cz[k] = pk2(bx[k].cz, bx[k].cz);
-    pf::group_thresholds(bx[k], gm, D[k], T[k]);
+    float T;
+    pf::group_thresholds(bx[k], gm, D[k], T);
+    nT[k] = -T;
   }
   uint32_t vis_n = 0, und_n = 0;
 #pragma unroll 1
-  for (int v = 0; v < nv; ++v) {
+  for (int v = nv - 1; v >= 0; --v) {
     const ulonglong2 ax0 = ws.qp[v][0][0], ax1 = ws.qp[v][0][1];
     const ulonglong2 ay0 = ws.qp[v][1][0], ay1 = ws.qp[v][1][1];
     const ulonglong2 az0 = ws.qp[v][2][0], az1 = ws.qp[v][2][1];
-    uint32_t in = 0, out = 0;
-#pragma unroll
-    for (int k = 0; k < kObjPerThread; ++k) {
-      // each axis' lo and hi plane values as one pair (the FMA chain of pf::plane)
-      float xl, xh, yl, yh, zl, zh;
-      upk2(fma2(cz[k], ax1.x, fma2(cy[k], ax0.y, fma2(cx[k], ax0.x, ax1.y))), xl, xh);
-      upk2(fma2(cz[k], ay1.x, fma2(cy[k], ay0.y, fma2(cx[k], ay0.x, ay1.y))), yl, yh);
-      upk2(fma2(cz[k], az1.x, fma2(cy[k], az0.y, fma2(cx[k], az0.x, az1.y))), zl, zh);
-      uint32_t vis, inv;
-      pf::decide_group(xl, xh, yl, yh, zl, zh, D[k], T[k], vis, inv);
-      in |= vis & (1u << k);
-      out |= inv & (1u << k);
-    }
-    const uint32_t und = ~(in | out) & 0xFu;
+    uint32_t in = VPP == 1 ? 0u : vis_n << 4, un = VPP == 1 ? 0u : und_n << 4;
+    decide_object<0>(cx, cy, cz, ax0, ax1, ay0, ay1, az0, az1, D, nT, in, un);
+    decide_object<1>(cx, cy, cz, ax0, ax1, ay0, ay1, az0, az1, D, nT, in, un);
+    decide_object<2>(cx, cy, cz, ax0, ax1, ay0, ay1, az0, az1, D, nT, in, un);
+    decide_object<3>(cx, cy, cz, ax0, ax1, ay0, ay1, az0, az1, D, nT, in, un);
     if (VPP == 1) {
-      // bit k of und -> bit 8k (the multiply places each bit k at 8k; the mask drops the
-      // cross terms)
-      und_n |= ((und & valid) * 0x204081u) & 0x01010101u;
+      // bit k of un -> bit 8k (the multiply places each bit k at 8k; the mask drops the
+      // cross terms); one view per pass, so v == 0
+      und_n |= ((un & valid) * 0x204081u) & 0x01010101u;
       store_nibble(ws, v, t, in & valid, lane);
     } else {
-      vis_n |= in << (4 * v);
-      und_n |= und << (4 * v);
+      vis_n = in;
+      und_n = un;
     }
   }
   if (VPP == 1) return und_n;

@@ -346,16 +346,36 @@ DPCULL_HD void group_thresholds(const Box& b, const GroupMargin& m, float& D, fl
   T = D + b.r;
 }
 
-// The group decision from the six plane values, as all-ones / zero masks.
-DPCULL_HD void decide_group(float xl, float xh, float yl, float yh, float zl, float zh, float D, float T,
-                            uint32_t& visible, uint32_t& invisible)
+// The group decision from the six plane values, as bits: ORs BIT into `visible` when the
+// pair is decided visible and into `undecided` when it is decided neither visible nor
+// invisible: visible if the smallest of the six plane values is above D, invisible if the
+// box is outside a lo plane, or outside a hi plane with every corner inside its lo plane
+// (the reference's `else if`), by T: o <= -T; a NaN comparison decides nothing.
+// negT = -T.  On the GPU each bit costs one comparison and one predicated OR (the
+// undecided comparison is "greater than or unordered", i.e. !(o <= -T), combined with
+// !vis in the same setp).
+template <uint32_t BIT>
+DPCULL_HD void decide_bits(float xl, float xh, float yl, float yh, float zl, float zh, float D, float negT,
+                           uint32_t& visible, uint32_t& undecided)
 {
   const float mlo = std::fmin(std::fmin(xl, yl), zl);
   const float mhi = std::fmin(std::fmin(xh, yh), zh);
   const float o = std::fmin(std::fmin(mlo, std::fmax(xh, -xl)),
                             std::fmin(std::fmax(yh, -yl), std::fmax(zh, -zl)));
-  visible = mask_gt(std::fmin(mlo, mhi), D);
-  invisible = mask_le(o, -T);
+  const float m6 = std::fmin(mlo, mhi);
+#if defined(__CUDA_ARCH__)
+  asm("{\n\t.reg .pred pv, pu;\n\t"
+      "setp.gt.f32 pv, %2, %3;\n\t"
+      "setp.gtu.and.f32 pu, %4, %5, !pv;\n\t"
+      "@pv or.b32 %0, %0, %6;\n\t"
+      "@pu or.b32 %1, %1, %6;\n\t}"
+      : "+r"(visible), "+r"(undecided)
+      : "f"(m6), "f"(D), "f"(o), "f"(negT), "n"(BIT));
+#else
+  const bool vis = m6 > D;
+  if (vis) visible |= BIT;
+  else if (!(o <= negT)) undecided |= BIT;
+#endif
 }
 
 // Whole classification of one box in one view of a group with margin m.
@@ -363,10 +383,10 @@ DPCULL_HD int classify_group(const Box& b, const Planes& p, const GroupMargin& m
 {
   float D, T;
   group_thresholds(b, m, D, T);
-  uint32_t vis, inv;
-  decide_group(plane(b, p.q[0][0]), plane(b, p.q[0][1]), plane(b, p.q[1][0]), plane(b, p.q[1][1]),
-               plane(b, p.q[2][0]), plane(b, p.q[2][1]), D, T, vis, inv);
-  return vis ? kVisible : inv ? kInvisible : kUndecided;
+  uint32_t vis = 0, und = 0;
+  decide_bits<1u>(plane(b, p.q[0][0]), plane(b, p.q[0][1]), plane(b, p.q[1][0]), plane(b, p.q[1][1]),
+                  plane(b, p.q[2][0]), plane(b, p.q[2][1]), D, -T, vis, und);
+  return vis ? kVisible : und ? kUndecided : kInvisible;
 }
 
 

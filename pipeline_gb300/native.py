@@ -59,6 +59,7 @@ _SIGS = {
     "dpcull_ctx_device_bytes": (C.c_uint64, [_P]),
     "dpcull_ctx_set_prefilter": (_I, [_P, _I]),
     "dpcull_ctx_set_box_cache": (_I, [_P, _I]),
+    "dpcull_ctx_cull_launches": (_I, [_P, C.POINTER(C.c_uint64)]),
     "dpcull_group_create": (_I, [_P, _UP]),
     "dpcull_group_destroy": (_I, [_P, _U32]),
     "dpcull_group_set_objects": (_I, [_P, _U32, _SZ, _FP, _FP, _UP]),
@@ -219,6 +220,12 @@ class Context:
     @property
     def kernel_launches(self) -> int:
         return int(self.lib.dpcull_ctx_kernel_launches(self.h))
+
+    def cull_launches(self) -> dict:
+        """Cull-kernel launches so far by kind: fused (no box cache), fill (stores it), read."""
+        out = (C.c_uint64 * 3)()
+        _check(self.lib.dpcull_ctx_cull_launches(self.h, out))
+        return {"fused": int(out[0]), "fill": int(out[1]), "read": int(out[2])}
 
     @property
     def device_bytes(self) -> int:

@@ -185,6 +185,50 @@ def test_one_group_in_two_jobs_of_one_launch(ctx):
     ctx.group_destroy(g)
 
 
+def test_kernel_kind_of_each_launch(ctx):
+    """Which cull kernel each plan launch runs: fused after a change, the storing one on
+    the next launch, the reading one from then on; the context's switch applies to a plan
+    created before it; every frame is the oracle's."""
+    rng = np.random.default_rng(47)
+    n, nm = 50_000, 900
+    lower, _, extent = W.random_boxes(rng, n)
+    mats = W.random_matrices(rng, nm)
+    mats[:, 12:15] *= np.float32(0.05)
+    xform = rng.integers(0, nm, n).astype(np.uint32)
+    g = ctx.group_create()
+    ctx.group_set_objects(g, lower, extent, xform)
+    ctx.group_set_matrices(g, mats)
+    vps = W.f32(W.cube_face_views()[:2])
+    rs = [ctx.result_create(g) for _ in vps]
+    p = ctx.plan_create([(g, rs, vps)], dict(views_per_pass=2, tiles_per_ticket=1, ctas_per_sm=0))
+
+    def launch(expect):
+        before = ctx.cull_launches()
+        ctx.plan_launch(p)
+        after = ctx.cull_launches()
+        got = [k for k in after if after[k] != before[k]]
+        assert got == [expect], (got, expect)
+        for r, vp in zip(rs, vps):
+            assert np.array_equal(ctx.result_bits(r), oracle.cull_bits(lower, extent, xform, mats, vp))
+
+    for kind in ("fused", "fill", "read", "read"):
+        launch(kind)
+    ctx.set_box_cache(False)
+    try:
+        launch("fused")
+        launch("fused")
+    finally:
+        ctx.set_box_cache(True)
+    launch("read")  # nothing changed while it was off
+    idx = np.array([3, 77, 899], np.uint32)
+    mats[idx] = W.random_matrices(rng, 3)
+    ctx.group_update_matrices(g, idx, mats)
+    for kind in ("fused", "fill", "read"):
+        launch(kind)
+    ctx.plan_destroy(p)
+    ctx.group_destroy(g)
+
+
 def test_stress_scene_cached_equals_uncached(ctx):
     """The stress distribution under 8 views over 6 launches of a plan: the words and
     changed lists with the cache (launch 2 stores it, launches 3-6 read it) equal those
