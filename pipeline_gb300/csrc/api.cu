@@ -569,9 +569,9 @@ int build_batch(dpcull_ctx c, const dpcull_job* jobs, size_t n_jobs, uint32_t vp
 }
 
 int persistent_grid(dpcull_ctx c, uint32_t vpp, uint32_t ctas_per_sm, uint32_t n_items,
-                    uint32_t per_ticket)
+                    uint32_t per_ticket, CacheMode mode)
 {
-  int occ = cull_max_ctas_per_sm((int)vpp);
+  int occ = cull_max_ctas_per_sm((int)vpp, mode);
   int per_sm = ctas_per_sm ? std::min<int>((int)ctas_per_sm, occ) : occ;
   const long long per_cta = (long long)per_ticket * kWarpsPerCta;  // each warp claims its own
   long long want = ((long long)n_items + per_cta - 1) / per_cta;
@@ -600,11 +600,12 @@ CacheMode batch_mode(dpcull_ctx c, const std::vector<uint32_t>& groups, const st
   return all_filled ? kCacheRead : all_culled ? kCacheFill : kCacheNone;
 }
 
-// Records a launch in the host record of every cached group it culled.
+// Records a launch in the host record of every cached group it culled (count: also in
+// the context's launch counts by kind).
 void note_launch(dpcull_ctx c, const std::vector<uint32_t>& groups, const std::vector<CullScene>& scenes,
-                 CacheMode mode)
+                 CacheMode mode, bool count = true)
 {
-  c->mode_launches[mode]++;
+  if (count) c->mode_launches[mode]++;
   for (size_t i = 0; i < scenes.size(); ++i)
     if (scenes[i].box) {
       Group& g = c->groups[groups[i]];
@@ -637,7 +638,7 @@ int launch_batch(dpcull_ctx c, const CullScene* d_scenes, const CullView* d_view
   a.exact_only = c->exact_only ? 1u : 0u;
   a.cache_mode = mode;
   a.ctl = c->ctl;
-  const int grid = persistent_grid(c, t.views_per_pass, t.ctas_per_sm, n_items, a.items_per_ticket);
+  const int grid = persistent_grid(c, t.views_per_pass, t.ctas_per_sm, n_items, a.items_per_ticket, mode);
   if (k0) CU(cudaEventRecordWithFlags(k0, s, cudaEventRecordExternal));
   if (launch_cull(a, grid, (int)t.views_per_pass, s)) return cuda_fail(cudaGetLastError(), "cull launch");
   if (k1) CU(cudaEventRecordWithFlags(k1, s, cudaEventRecordExternal));
@@ -661,14 +662,18 @@ std::string tune_key(const std::vector<CullScene>& scenes, const std::vector<Cul
 {
   uint64_t objs = 0;
   uint32_t maxv = 0;
+  bool cached = !scenes.empty();
   for (auto& s : scenes) {
     objs += s.n_objects;
     maxv = std::max(maxv, s.n_views);
+    cached = cached && s.box;
   }
   const int bucket = objs ? (int)std::floor(std::log2((double)objs)) : 0;
-  char buf[96];
-  // "w512": tunings of the kernel whose warp items are 512 objects
-  snprintf(buf, sizeof buf, "w512_n2^%d_v%zu_maxv%u_s%zu", bucket, views.size(), maxv, scenes.size());
+  char buf[112];
+  // "w512": tunings of the kernel whose warp items are 512 objects; "bc": of the kernel
+  // that reads the box caches (the steady state of a plan whose scenes all keep one)
+  snprintf(buf, sizeof buf, "w512_n2^%d_v%zu_maxv%u_s%zu%s", bucket, views.size(), maxv, scenes.size(),
+           cached ? "_bc" : "");
   return buf;
 }
 
@@ -1157,7 +1162,7 @@ int dpcull_cull(dpcull_ctx c, dpcull_group gh, dpcull_result rh, const float vp[
   a.one_view = view_of(*r, vp);
   a.item_tiles = item_tiles_for(a.one_scene.n_tiles, c->sm_count);
   a.n_items = items_of(a.one_scene.n_tiles, 1, a.item_tiles);
-  const int grid = persistent_grid(c, 1, 0, a.n_items, 1);
+  const int grid = persistent_grid(c, 1, 0, a.n_items, 1, mode);
   if (launch_cull(a, grid, 1, c->stream)) return cuda_fail(cudaGetLastError(), "cull launch");
   if (launch_changed_lists(nullptr, a.one_view, 1, a.one_view.n_words, c->stream))
     return cuda_fail(cudaGetLastError(), "changed-list launch");
@@ -1331,15 +1336,17 @@ static int plan_capture(dpcull_ctx c, Plan& p, int slot, CacheMode mode)
 
 static int time_batch(dpcull_ctx c, const CullScene* ds, const CullView* dv,
                       const std::vector<CullScene>& sc, const std::vector<CullView>& vw,
-                      uint32_t items, uint32_t item_tiles, const dpcull_tuning& t, int reps, float* ms)
+                      uint32_t items, uint32_t item_tiles, const dpcull_tuning& t, int reps, float* ms,
+                      CacheMode mode)
 {
   cudaEvent_t e0, e1;
   CU(cudaEventCreate(&e0));
   CU(cudaEventCreate(&e1));
   const uint32_t nvw = (uint32_t)vw.size();
-  int rc = launch_batch(c, ds, dv, sc, nvw, items, item_tiles, t, c->stream);  // warm-up
+  int rc = launch_batch(c, ds, dv, sc, nvw, items, item_tiles, t, c->stream, nullptr, nullptr, mode);  // warm-up
   if (!rc) cudaEventRecord(e0, c->stream);
-  for (int i = 0; i < reps && !rc; ++i) rc = launch_batch(c, ds, dv, sc, nvw, items, item_tiles, t, c->stream);
+  for (int i = 0; i < reps && !rc; ++i)
+    rc = launch_batch(c, ds, dv, sc, nvw, items, item_tiles, t, c->stream, nullptr, nullptr, mode);
   if (!rc) {
     cudaEventRecord(e1, c->stream);
     cudaEventSynchronize(e1);
@@ -1380,13 +1387,20 @@ int dpcull_autotune(dpcull_ctx c, const dpcull_job* jobs, size_t n_jobs, dpcull_
     }
   dpcull_tuning best{(uint32_t)default_vpp(maxv), 1, 0, 0};
   float best_ms = 1e30f;
+  // The kernel a plan of these jobs runs from its third launch on: the one that reads the
+  // box caches when every scene keeps one (stored here first by one Fill launch, as a plan's
+  // second launch would), the fused one otherwise.
+  bool cached = c->box_cache && !c->exact_only && !scenes.empty();
+  for (const CullScene& sc : scenes) cached = cached && sc.box;
+  bool filled = false;
   const uint32_t vpps[4] = {1, 2, 4, 8};
   for (uint32_t vpp : vpps) {
     if (vpp > 1 && vpp / 2 >= maxv) continue;  // wider passes than any scene has views
     std::vector<CullScene> sc;
     std::vector<CullView> vw;
+    std::vector<uint32_t> groups;
     uint32_t it_items = 0, it_tiles = kItemTiles;
-    rc = build_batch(c, jobs, n_jobs, vpp, sc, vw, &it_items, nullptr, nullptr, &it_tiles);
+    rc = build_batch(c, jobs, n_jobs, vpp, sc, vw, &it_items, &groups, nullptr, &it_tiles);
     if (rc || !it_items) break;
     CullScene* ds = nullptr;
     CullView* dv = nullptr;
@@ -1396,12 +1410,21 @@ int dpcull_autotune(dpcull_ctx c, const dpcull_job* jobs, size_t n_jobs, dpcull_
     }
     cudaMemcpyAsync(ds, sc.data(), sc.size() * sizeof(CullScene), cudaMemcpyHostToDevice, c->stream);
     cudaMemcpyAsync(dv, vw.data(), vw.size() * sizeof(CullView), cudaMemcpyHostToDevice, c->stream);
-    const int occ = cull_max_ctas_per_sm((int)vpp);
+    if (cached && !filled) {
+      const dpcull_tuning ft{vpp, 1, 0, 0};
+      rc = launch_batch(c, ds, dv, sc, (uint32_t)vw.size(), it_items, it_tiles, ft, c->stream, nullptr, nullptr,
+                        kCacheFill);
+      if (rc) break;
+      note_launch(c, groups, sc, kCacheFill, false);
+      filled = true;
+    }
+    const CacheMode mode = cached ? kCacheRead : kCacheNone;
+    const int occ = cull_max_ctas_per_sm((int)vpp, mode);
     for (uint32_t tpt : {1u, 2u, 4u}) {
       for (int cps = 1; cps <= occ; ++cps) {
         dpcull_tuning t{vpp, tpt, (uint32_t)cps, 0};
         float ms = 0;
-        rc = time_batch(c, ds, dv, sc, vw, it_items, it_tiles, t, 3, &ms);
+        rc = time_batch(c, ds, dv, sc, vw, it_items, it_tiles, t, 3, &ms, mode);
         if (rc) break;
         if (ms < best_ms) {
           best_ms = ms;

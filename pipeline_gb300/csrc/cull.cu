@@ -387,6 +387,13 @@ __device__ __forceinline__ uint32_t classify_tile(const CullLaunch& a, WarpShare
     pf::Box bx[kObjPerThread];
     uint32_t amb;
     if (cache_ok) {
+      // The next tile's boxes into L1 while this tile is classified (5 x 512 bytes per
+      // warp; the loads below of the tile after hit there).
+      if (t + 1 < n_t) {
+        const float* nb = sc.box + obj0 + kTileObjects;
+#pragma unroll
+        for (int r = 0; r < kBoxRows; ++r) asm volatile("prefetch.global.L1 [%0];" ::"l"(nb + r * cap));
+      }
       const uint32_t valid = cached_boxes(sc, obj0, bx);
       amb = classify_views<VPP>(ws, bx, nv, t, valid, lane);
     } else {
@@ -592,8 +599,10 @@ __device__ __forceinline__ void warp_item(const CullLaunch& a, uint32_t item, Wa
   finish_item<VPP>(ws, tile_first, n_t, nv, lane);
 }
 
+// The kernels that transform the boxes hold 80 registers (3 CTAs of 256 threads per SM);
+// the one that reads the box cache needs fewer and runs at 4.
 template <int VPP, bool PF, bool WIDE, uint32_t MODE>
-__global__ void __launch_bounds__(kThreads, 3) cull_kernel(const __grid_constant__ CullLaunch a)
+__global__ void __launch_bounds__(kThreads, MODE == kCacheRead ? 4 : 3) cull_kernel(const __grid_constant__ CullLaunch a)
 {
   __shared__ WarpShared wsh[kThreads / 32];
   WarpShared& ws = wsh[threadIdx.x >> 5];
@@ -755,14 +764,24 @@ int launch_vpp(const CullLaunch& a, int grid, cudaStream_t s)
   return cudaGetLastError() == cudaSuccess ? 0 : -1;
 }
 
-template <int VPP>
+template <int VPP, uint32_t MODE>
 int max_ctas()
 {
+  static int cached = 0;  // the same for every GB300; a race only writes the same value
+  if (cached) return cached;
   int n = 0;
-  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, cull_kernel<VPP, true, true, kCacheNone>, kThreads, 0) !=
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, cull_kernel<VPP, true, true, MODE>, kThreads, 0) !=
       cudaSuccess)
     return 1;
-  return n > 0 ? n : 1;
+  cached = n > 0 ? n : 1;
+  return cached;
+}
+
+template <int VPP>
+int max_ctas_mode(uint32_t mode)
+{
+  return mode == kCacheRead ? max_ctas<VPP, kCacheRead>() : mode == kCacheFill ? max_ctas<VPP, kCacheFill>()
+                                                                               : max_ctas<VPP, kCacheNone>();
 }
 
 // ---- small helper kernels -----------------------------------------------------------
@@ -816,13 +835,13 @@ int launch_cull(const CullLaunch& args, int grid, int vpp, void* stream)
   }
 }
 
-int cull_max_ctas_per_sm(int vpp)
+int cull_max_ctas_per_sm(int vpp, uint32_t mode)
 {
   switch (vpp) {
-    case 1: return max_ctas<1>();
-    case 2: return max_ctas<2>();
-    case 4: return max_ctas<4>();
-    case 8: return max_ctas<8>();
+    case 1: return max_ctas_mode<1>(mode);
+    case 2: return max_ctas_mode<2>(mode);
+    case 4: return max_ctas_mode<4>(mode);
+    case 8: return max_ctas_mode<8>(mode);
     default: return 1;
   }
 }

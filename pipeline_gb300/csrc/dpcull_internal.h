@@ -138,7 +138,8 @@ struct CullLaunch {
 
 // Launchers (cull.cu).  vpp = views per pass (1, 2, 4 or 8).
 int launch_cull(const CullLaunch& args, int grid, int vpp, void* stream);
-int cull_max_ctas_per_sm(int vpp);
+// CTAs of the cull kernel of this kind (CacheMode) that fit on one SM.
+int cull_max_ctas_per_sm(int vpp, uint32_t mode);
 // Changed-list assembly after a cull launch over `n_views` views (device array `views`,
 // or the single `one` when views is null): per-chunk counts of the delta words, then the
 // emission of every changed index into the packed ascending list.  max_words bounds

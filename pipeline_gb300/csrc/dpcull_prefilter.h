@@ -340,6 +340,8 @@ DPCULL_HD GroupMargin merge(const GroupMargin& a, const GroupMargin& b)
 }
 
 // Thresholds of one box against a group margin (NaN when the box cannot be bounded).
+// D >= +0 otherwise: d0, the group's kappa and g are never negative (unbounded views
+// contribute zeros to the margin), so D is an FMA of non-negative terms.
 DPCULL_HD void group_thresholds(const Box& b, const GroupMargin& m, float& D, float& T)
 {
   D = std::fma(b.d0, m.k, m.g);
@@ -348,31 +350,31 @@ DPCULL_HD void group_thresholds(const Box& b, const GroupMargin& m, float& D, fl
 
 // The group decision from the six plane values, as bits: ORs BIT into `visible` when the
 // pair is decided visible and into `undecided` when it is decided neither visible nor
-// invisible: visible if the smallest of the six plane values is above D, invisible if the
-// box is outside a lo plane, or outside a hi plane with every corner inside its lo plane
-// (the reference's `else if`), by T: o <= -T; a NaN comparison decides nothing.
-// negT = -T.  On the GPU each bit costs one comparison and one predicated OR (the
-// undecided comparison is "greater than or unordered", i.e. !(o <= -T), combined with
-// !vis in the same setp).
+// invisible.  Visible if all six plane values are above D; invisible if the box is outside
+// a lo plane, or outside a hi plane with every corner inside its lo plane (the reference's
+// `else if`), by T: o <= -T with o = min(xl, yl, zl, max(xh, -xl), max(yh, -yl),
+// max(zh, -zl)); a NaN comparison decides nothing.  One value serves both tests: D >= 0
+// (or NaN), and then "all six > D" <=> o > D (if every value is above D >= 0, each -lo is
+// negative and each max(hi, -lo) is hi; if o > D, every lo value is above 0, so each
+// max(hi, -lo) above D is hi).  negT = -T.  On the GPU each bit costs one comparison and
+// one predicated OR (the undecided comparison is "greater than or unordered", i.e.
+// !(o <= -T), combined with !vis in the same setp).
 template <uint32_t BIT>
 DPCULL_HD void decide_bits(float xl, float xh, float yl, float yh, float zl, float zh, float D, float negT,
                            uint32_t& visible, uint32_t& undecided)
 {
-  const float mlo = std::fmin(std::fmin(xl, yl), zl);
-  const float mhi = std::fmin(std::fmin(xh, yh), zh);
-  const float o = std::fmin(std::fmin(mlo, std::fmax(xh, -xl)),
+  const float o = std::fmin(std::fmin(std::fmin(xl, yl), std::fmin(zl, std::fmax(xh, -xl))),
                             std::fmin(std::fmax(yh, -yl), std::fmax(zh, -zl)));
-  const float m6 = std::fmin(mlo, mhi);
 #if defined(__CUDA_ARCH__)
   asm("{\n\t.reg .pred pv, pu;\n\t"
       "setp.gt.f32 pv, %2, %3;\n\t"
-      "setp.gtu.and.f32 pu, %4, %5, !pv;\n\t"
-      "@pv or.b32 %0, %0, %6;\n\t"
-      "@pu or.b32 %1, %1, %6;\n\t}"
+      "setp.gtu.and.f32 pu, %2, %4, !pv;\n\t"
+      "@pv or.b32 %0, %0, %5;\n\t"
+      "@pu or.b32 %1, %1, %5;\n\t}"
       : "+r"(visible), "+r"(undecided)
-      : "f"(m6), "f"(D), "f"(o), "f"(negT), "n"(BIT));
+      : "f"(o), "f"(D), "f"(negT), "n"(BIT));
 #else
-  const bool vis = m6 > D;
+  const bool vis = o > D;
   if (vis) visible |= BIT;
   else if (!(o <= negT)) undecided |= BIT;
 #endif

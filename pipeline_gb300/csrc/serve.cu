@@ -421,7 +421,7 @@ bool launch(dpcull_server s, Slot& slot)
   for (size_t i = 0; i < take.size(); ++i)
     if ((uintptr_t)slot.h_scenes[i].mats & 31u) a.wide_mats = 0;
   a.ctl = slot.ctl;
-  const int occ = cull_max_ctas_per_sm(vpp);
+  const int occ = cull_max_ctas_per_sm(vpp, kCacheNone);  // served scenes keep no box cache
   const long long want = ((long long)items + kWarpsPerCta - 1) / kWarpsPerCta;  // a warp per item
   const int grid = (int)std::max<long long>(1, std::min<long long>((long long)s->sm_count * occ, want));
   launch_cull(a, grid, vpp, slot.stream);
