@@ -559,10 +559,7 @@ int build_batch(dpcull_ctx c, const dpcull_job* jobs, size_t n_jobs, uint32_t vp
   uint64_t tile_groups = 0;
   for (auto& s : scenes) tile_groups += (uint64_t)s.n_tiles * s.n_vgroups;
   const uint32_t it = item_tiles_for(tile_groups, c->sm_count);
-  for (auto& s : scenes) {
-    s.item_begin = items;
-    items += items_of(s.n_tiles, s.n_vgroups, it);
-  }
+  items = lay_out_items(scenes.data(), scenes.size(), it, tail_units(c->sm_count));
   *n_items = items;
   if (item_tiles_out) *item_tiles_out = it;
   return DPCULL_OK;
@@ -1161,7 +1158,7 @@ int dpcull_cull(dpcull_ctx c, dpcull_group gh, dpcull_result rh, const float vp[
   a.cache_mode = mode;
   a.one_view = view_of(*r, vp);
   a.item_tiles = item_tiles_for(a.one_scene.n_tiles, c->sm_count);
-  a.n_items = items_of(a.one_scene.n_tiles, 1, a.item_tiles);
+  a.n_items = lay_out_items(&a.one_scene, 1, a.item_tiles, tail_units(c->sm_count));
   const int grid = persistent_grid(c, 1, 0, a.n_items, 1, mode);
   if (launch_cull(a, grid, 1, c->stream)) return cuda_fail(cudaGetLastError(), "cull launch");
   if (launch_changed_lists(nullptr, a.one_view, 1, a.one_view.n_words, c->stream))

@@ -530,7 +530,7 @@ __device__ __forceinline__ void warp_item(const CullLaunch& a, uint32_t item, Wa
   const int lane = threadIdx.x & 31;
   __syncwarp();  // the previous item's reads of the shared state are done
   if ((uint64_t)(item - ws.sc.item_begin) >=
-      (uint64_t)items_of(ws.sc.n_tiles, ws.sc.n_vgroups, a.item_tiles)) {
+      (uint64_t)tile_groups_of(ws.sc.n_tiles, ws.sc.n_big, a.item_tiles) * ws.sc.n_vgroups) {
     const CullScene* src = a.scenes ? a.scenes + find_scene(a.scenes, a.n_scenes, item) : &a.one_scene;
     constexpr int kSceneWords = (int)(sizeof(CullScene) / 4);
     if (lane < kSceneWords) reinterpret_cast<uint32_t*>(&ws.sc)[lane] = reinterpret_cast<const uint32_t*>(src)[lane];
@@ -545,8 +545,9 @@ __device__ __forceinline__ void warp_item(const CullLaunch& a, uint32_t item, Wa
   const uint32_t group = local / sc.n_vgroups;
   const uint32_t vfirst = (local - group * sc.n_vgroups) * VPP;
   const int nv = (int)min((uint32_t)VPP, sc.n_views - vfirst);
-  const uint32_t tile_first = group * a.item_tiles;
-  const uint32_t n_t = min(a.item_tiles, sc.n_tiles - tile_first);
+  const bool big = group < sc.n_big;  // else one of the scene's single-tile items
+  const uint32_t tile_first = big ? group * a.item_tiles : sc.n_big * a.item_tiles + (group - sc.n_big);
+  const uint32_t n_t = big ? min(a.item_tiles, sc.n_tiles - tile_first) : 1u;
   // The cached kernel reads the scene's cache state once per item (it does not change
   // during a launch); the other kernels load the first tile's transform indices while the
   // views are staged.
@@ -611,6 +612,7 @@ __global__ void __launch_bounds__(kThreads, MODE == kCacheRead ? 4 : 3) cull_ker
   if (threadIdx.x % 32 == 0) {
     ws.sc.item_begin = 0;  // no scene cached: the first item looks its scene up
     ws.sc.n_tiles = 0;
+    ws.sc.n_big = 0;
     ws.sc.n_vgroups = 1;
   }
   uint32_t vkey = ~0u;

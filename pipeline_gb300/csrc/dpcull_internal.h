@@ -42,6 +42,16 @@ DPCULL_HD_CONST uint32_t items_of(uint32_t n_tiles, uint32_t n_vgroups, uint32_t
   return (n_tiles + item_tiles - 1) / item_tiles * n_vgroups;
 }
 
+// With a tail: the scene's first n_big tile groups have item_tiles tiles (the last of them
+// may be short), every tile after them is a group of its own.  Any n_big from 0 to
+// ceil(n_tiles / item_tiles) covers every tile once; the launch hands the items out in
+// order, so single-tile items at the end of a launch shorten the time the warps that
+// finish first wait for the last ones.
+DPCULL_HD_CONST uint32_t tile_groups_of(uint32_t n_tiles, uint32_t n_big, uint32_t item_tiles)
+{
+  return n_big + (n_tiles > n_big * item_tiles ? n_tiles - n_big * item_tiles : 0u);
+}
+
 // Tiles per work item for a launch of `tile_groups` (tiles x view groups) on `sm_count`
 // SMs: long items amortise each warp's exact drain, short ones keep every warp busy when
 // the launch is small.
@@ -93,8 +103,37 @@ struct CullScene {
   uint32_t n_views;
   uint32_t n_vgroups;      // ceil(n_views / views per pass)
   uint32_t n_tiles;
-  uint32_t item_begin;     // first work item of this scene (items_of(n_tiles, n_vgroups, ...))
+  uint32_t item_begin;     // first work item of this scene (scene_items)
+  uint32_t n_big;          // tile groups of item_tiles tiles; the tiles after them are one per item
 };
+
+// Host: the item layout of a launch over `n` scenes with `item_tiles` tiles per item.
+// The launch's last `tail` (tile x view group) units become single-tile items (walking
+// from the last scene back); every other scene keeps items of item_tiles tiles.  Sets
+// every scene's n_big and item_begin; returns the launch's item count.
+inline uint32_t lay_out_items(CullScene* scenes, size_t n, uint32_t item_tiles, uint64_t tail)
+{
+  for (size_t k = n; k-- > 0;) {
+    CullScene& s = scenes[k];
+    const uint64_t per = s.n_vgroups ? s.n_vgroups : 1u;
+    uint32_t singles = 0;
+    if (item_tiles > 1 && tail) {
+      const uint64_t want = (tail + per - 1) / per;
+      singles = want < s.n_tiles ? (uint32_t)want : s.n_tiles;
+      tail -= (uint64_t)singles * per < tail ? (uint64_t)singles * per : tail;
+    }
+    s.n_big = singles ? (s.n_tiles - singles) / item_tiles : (s.n_tiles + item_tiles - 1) / item_tiles;
+  }
+  uint32_t items = 0;
+  for (size_t k = 0; k < n; ++k) {
+    scenes[k].item_begin = items;
+    items += tile_groups_of(scenes[k].n_tiles, scenes[k].n_big, item_tiles) * scenes[k].n_vgroups;
+  }
+  return items;
+}
+
+// Single-tile units at the end of a launch: about two per warp that can be resident.
+inline uint64_t tail_units(int sm_count) { return (uint64_t)(sm_count > 0 ? sm_count : 1) * 64u; }
 
 struct alignas(16) CullView {   // 128 bytes; staged whole into shared memory by the cull
   float vp[16];

@@ -129,7 +129,7 @@ extern "C" int dpcull_cull_noalloc(const float* objects, size_t cap, size_t n, c
   int sms = 0;
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
   a.item_tiles = item_tiles_for(tiles, sms);
-  a.n_items = items_of(tiles, 1, a.item_tiles);
+  a.n_items = lay_out_items(&a.one_scene, 1, a.item_tiles, tail_units(sms));
   const int grid = (int)((a.n_items + kWarpsPerCta - 1) / kWarpsPerCta);  // one item per warp
   if (launch_cull(a, grid, 1, st) || launch_changed_lists(nullptr, a.one_view, 1, a.one_view.n_words, st)) {
     cudaGetLastError();

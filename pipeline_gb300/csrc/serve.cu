@@ -388,6 +388,7 @@ bool launch(dpcull_server s, Slot& slot)
     cs.n_views = q.n_views;
     cs.n_vgroups = (q.n_views + vpp - 1) / vpp;
     cs.n_tiles = (uint32_t)(sc.cap / kTileObjects);
+    cs.n_big = (cs.n_tiles + item_tiles - 1) / item_tiles;  // every item item_tiles long
     cs.item_begin = items;
     items += items_of(cs.n_tiles, cs.n_vgroups, item_tiles);
     max_tiles = std::max(max_tiles, cs.n_tiles);
