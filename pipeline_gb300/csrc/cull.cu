@@ -485,36 +485,48 @@ __device__ __forceinline__ uint32_t classify_tile(const CullLaunch& a, WarpShare
 }
 
 // The final words of the item, per view: the new words (stored only where they changed),
-// the delta words (old XOR new, every word) and the visible count.  Lane l handles word
-// l & 3 of tile l >> 2, so a view's words are one coalesced load and store.  Every view's
-// previous words are loaded before any store, so the loads are in flight together.
+// the delta words (old XOR new, every word) and, for serving launches, the visible count.
+// The lanes take (view, word) pairs: a view's words occupy 16 lanes (4 for a single-tile
+// item), so 2 (8) views go per pass and the 8 views of an item take 4 passes (1).  Every
+// pass's previous words are loaded before any store, so the loads are in flight together.
 template <int VPP>
 __device__ __forceinline__ void finish_item(const WarpShared& ws, uint32_t tile_first, uint32_t n_t,
                                             int nv, int lane)
 {
-  const bool mine = (uint32_t)lane < n_t * kTileWords;
-  const uint32_t word = tile_first * kTileWords + (uint32_t)lane;
-  uint32_t prev[VPP];
+  constexpr int kPasses = (VPP * kItemTiles * kTileWords + 31) / 32;
+  const uint32_t wpv = n_t * kTileWords;  // the item's words per view
+  const int sh = n_t == 1 ? 2 : 4;        // lanes per view: 4 or 16
+  const uint32_t base = tile_first * kTileWords;
+  uint32_t prev[kPasses];
 #pragma unroll
-  for (int v = 0; v < VPP; ++v)
-    prev[v] = (v < nv && mine && !(ws.cv[v].flags & kViewNoChanged)) ? ws.cv[v].bits[word] : 0u;
+  for (int i = 0; i < kPasses; ++i) {
+    const uint32_t p = (uint32_t)lane + 32u * i, v = p >> sh, wd = p & ((1u << sh) - 1u);
+    const bool act = v < (uint32_t)nv && wd < wpv;
+    prev[i] = act && !(ws.cv[v].flags & kViewNoChanged) ? ws.cv[v].bits[base + wd] : 0u;
+  }
 #pragma unroll
-  for (int v = 0; v < VPP; ++v) {
-    if (v < nv) {
+  for (int i = 0; i < kPasses; ++i) {
+    const uint32_t p = (uint32_t)lane + 32u * i, v = p >> sh, wd = p & ((1u << sh) - 1u);
+    if (v < (uint32_t)nv && wd < wpv) {
       const CullView& cv = ws.cv[v];
-      const uint32_t w = mine ? (&ws.words[v][0][0])[lane] : 0u;
-      if (mine) {
-        if (cv.flags & kViewNoChanged) {
-          cv.bits[word] = w;
-        } else {
-          const uint32_t d = w ^ prev[v];
-          if (d) cv.bits[word] = w;
-          cv.delta[word] = d;
-        }
+      const uint32_t w = (&ws.words[v][0][0])[wd];
+      if (cv.flags & kViewNoChanged) {
+        cv.bits[base + wd] = w;
+      } else {
+        const uint32_t d = w ^ prev[i];
+        if (d) cv.bits[base + wd] = w;
+        cv.delta[base + wd] = d;
       }
-      if (cv.n_visible) {
+    }
+  }
+  if (ws.cv[0].n_visible) {  // serving launches count every view's visible objects
+    const bool mine = (uint32_t)lane < wpv;
+#pragma unroll
+    for (int v = 0; v < VPP; ++v) {
+      if (v < nv && ws.cv[v].n_visible) {
+        const uint32_t w = mine ? (&ws.words[v][0][0])[lane] : 0u;
         const uint32_t cnt = __reduce_add_sync(0xffffffffu, (uint32_t)__popc(w));
-        if (lane == 0 && cnt) atomicAdd(cv.n_visible, cnt);
+        if (lane == 0 && cnt) atomicAdd(ws.cv[v].n_visible, cnt);
       }
     }
   }
