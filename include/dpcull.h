@@ -218,7 +218,11 @@ int dpcull_plan_read_async(dpcull_ctx ctx, dpcull_plan p, uint32_t* const* bits,
                            uint32_t* const* changed, const size_t* changed_cap, size_t* n_changed);
 /* Snapshots the results of the plan's last launch on the device and starts copying their
  * changed counts to the host, without waiting; the next dpcull_plan_read_async reads this
- * snapshot.  A later dpcull_plan_launch may overwrite the results themselves. */
+ * snapshot.  A later dpcull_plan_launch may overwrite the results themselves.  From the
+ * first snapshot or asynchronous read on, every launch of the plan also writes its results
+ * into a second buffer of its own (one per graph slot), so the snapshot of a launch costs
+ * no copy on the device; a launch made before that, or made while an unread snapshot holds
+ * its buffer, is snapshotted by one copy of the results. */
 int dpcull_plan_snapshot(dpcull_ctx ctx, dpcull_plan p);
 int dpcull_plan_read_wait(dpcull_ctx ctx, dpcull_plan p);
 int dpcull_plan_destroy(dpcull_ctx ctx, dpcull_plan p);

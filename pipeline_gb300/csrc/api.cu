@@ -140,21 +140,31 @@ struct Plan {
   bool fresh[2] = {false, false};      // slot holds matrices from set_views
   std::vector<uint32_t> all_groups;    // every job's group (empty ones included)
   std::vector<uint32_t> all_results;   // every job's results, in job and view order
-  uint32_t* h_counts = nullptr;        // pinned: changed counts of the snapshot (read_async)
+  uint32_t* h_counts = nullptr;        // pinned: changed counts of the snapshot (read_async),
+                                       // then the device error word pair
   uint32_t* h_rcounts = nullptr;       // pinned: changed counts read by dpcull_plan_read, apart
                                        // from a pending snapshot's, which it must not overwrite
-  // dpcull_plan_read_async: device snapshots of the results, copied out on copy_stream
+  // Asynchronous reads (dpcull_plan_snapshot / _read_async).  Once the first one is asked
+  // for, every launch also writes its results into the copy buffer of its slot (the views'
+  // copy pointers), and a read copies a launch's buffer to the host on copy_stream while
+  // the next launch runs.  Slot layout: the results' changed counts (one word each), then
+  // per result its words and its changed list (snap_bits / snap_changed offsets).
+  bool copies = false;                 // the buffers exist and the views point at them
+  uint32_t* cbuf[2] = {nullptr, nullptr};
+  bool copied[2] = {false, false};     // the slot's buffer holds its last launch's results
+  bool copying[2] = {false, false};    // the slot's views carry the copy pointers
+  bool read_pending[2] = {false, false};  // copies out of the slot issued, not yet waited for
+  int snap_slot = -1;                  // the slot the pending snapshot reads
   cudaStream_t copy_stream = nullptr;
-  cudaEvent_t snap_ev = nullptr, counts_ev = nullptr, copies_ev = nullptr;
-  bool read_pending = false;           // copies issued, not yet waited for
+  cudaEvent_t snap_ev = nullptr, counts_ev = nullptr;
+  cudaEvent_t copies_ev[2] = {nullptr, nullptr};
   bool snap_pending = false;           // snapshot taken (dpcull_plan_snapshot), not yet read
-  ResultCopy* d_copies = nullptr;      // one per result
-  uint32_t* snap = nullptr;            // words and changed lists of every result
-  uint32_t* d_counts = nullptr;        // changed counts, then the device error word pair
-  size_t snap_words = 0;
+  ResultCopy* d_copies = nullptr;      // per slot, one per result: live results -> slot buffer
+  size_t snap_words = 0;               // words per slot buffer
   uint32_t snap_max_len = 0;
-  std::vector<size_t> snap_bits, snap_changed;  // offsets into snap
+  std::vector<size_t> snap_bits, snap_changed;  // offsets into a slot buffer
   std::vector<size_t> snap_sizes;      // each result's size at set-up
+  std::vector<int> view_result;        // result index (in all_results) of each launched view
   std::vector<uint64_t> all_incarnations;
   int next = 0;
   dpcull_tuning tuning{};
@@ -1512,6 +1522,8 @@ int dpcull_plan_set_views(dpcull_ctx c, dpcull_plan ph, const float* vps)
   return DPCULL_OK;
 }
 
+static void plan_slot_copying(Plan* p, int s, bool on);
+
 int dpcull_plan_launch(dpcull_ctx c, dpcull_plan ph)
 {
   Plan* p = get_plan(c, ph);
@@ -1537,6 +1549,14 @@ int dpcull_plan_launch(dpcull_ctx c, dpcull_plan ph)
     for (size_t v = 0; v < p->views.size(); ++v) memcpy(p->h_views[s][v].vp, p->views[v].vp, 64);
   }
   p->fresh[s] = false;
+  if (p->copies) {
+    // The launch writes its results into the slot's copy buffer too, unless a snapshot
+    // still waits to be read from it; copies still reading the buffer finish first.
+    const bool hold = p->snap_pending && p->snap_slot == s;
+    plan_slot_copying(p, s, !hold);
+    p->copied[s] = !hold;
+    if (!hold && p->read_pending[s]) CU(cudaStreamWaitEvent(c->stream, p->copies_ev[s], 0));
+  }
   const CacheMode mode = batch_mode(c, p->groups, p->scenes);
   if (!p->exec[mode][s]) {
     int rc = plan_capture(c, *p, s, mode);
@@ -1600,28 +1620,35 @@ int dpcull_plan_read(dpcull_ctx c, dpcull_plan ph, uint32_t* const* bits, uint32
   return DPCULL_OK;
 }
 
-// Device snapshot storage and descriptors of a plan's results (set up on first use, and
-// again when a result's size changed).
-static int plan_snapshot_setup(dpcull_ctx c, Plan* p, const std::vector<Result*>& rs)
+// The copy buffers of a plan's results, one per slot (set up on the first asynchronous
+// read, and again when a result's size changed), and the views' copy pointers.
+static int plan_copies_setup(dpcull_ctx c, Plan* p, const std::vector<Result*>& rs)
 {
   const size_t nr = rs.size();
-  bool same = p->snap && p->snap_sizes.size() == nr;
+  bool same = p->copies && p->snap_sizes.size() == nr;
   for (size_t i = 0; same && i < nr; ++i) same = p->snap_sizes[i] == rs[i]->size_bits;
   if (same) return DPCULL_OK;
-  if (p->read_pending) CU(cudaEventSynchronize(p->copies_ev));
-  p->read_pending = false;
-  p->snap_pending = false;
+  // Nothing may still read the old buffers or launch with views that point at them.
+  for (int s = 0; s < 2; ++s)
+    if (p->read_pending[s]) CU(cudaEventSynchronize(p->copies_ev[s]));
   CU(cudaStreamSynchronize(c->stream));
-  dfree(c, p->snap, p->snap_words * 4);
-  dfree(c, p->d_copies, p->snap_sizes.size() * sizeof(ResultCopy));
-  dfree(c, p->d_counts, (p->snap_sizes.size() + 2) * 4);
-  p->snap = nullptr;
+  for (int s = 0; s < 2; ++s) {
+    p->read_pending[s] = p->copied[s] = p->copying[s] = false;
+    dfree(c, p->cbuf[s], p->snap_words * 4);
+    p->cbuf[s] = nullptr;
+    for (size_t v = 0; v < p->views.size(); ++v) {
+      p->h_views[s][v].copy_bits = p->h_views[s][v].copy_changed = p->h_views[s][v].copy_count = nullptr;
+    }
+  }
+  dfree(c, p->d_copies, p->snap_sizes.size() * 2 * sizeof(ResultCopy));
   p->d_copies = nullptr;
-  p->d_counts = nullptr;
+  p->copies = false;
+  p->snap_pending = false;
+  p->snap_slot = -1;
   p->snap_sizes.assign(nr, 0);
   p->snap_bits.assign(nr, 0);
   p->snap_changed.assign(nr, 0);
-  size_t total = 0;
+  size_t total = (nr + 63) / 64 * 64;  // the counts
   uint32_t max_len = 1;
   for (size_t i = 0; i < nr; ++i) {
     const size_t n = rs[i]->size_bits, words = (n + 31) / 32;
@@ -1634,21 +1661,50 @@ static int plan_snapshot_setup(dpcull_ctx c, Plan* p, const std::vector<Result*>
   }
   p->snap_words = std::max<size_t>(total, 64);
   p->snap_max_len = max_len;
-  int rc = dalloc(c, (void**)&p->snap, p->snap_words * 4);
-  if (!rc) rc = dalloc(c, (void**)&p->d_copies, std::max<size_t>(nr, 1) * sizeof(ResultCopy));
-  if (!rc) rc = dalloc(c, (void**)&p->d_counts, (nr + 2) * 4);
+  int rc = dalloc(c, (void**)&p->cbuf[0], p->snap_words * 4);
+  if (!rc) rc = dalloc(c, (void**)&p->cbuf[1], p->snap_words * 4);
+  if (!rc) rc = dalloc(c, (void**)&p->d_copies, std::max<size_t>(2 * nr, 1) * sizeof(ResultCopy));
   if (rc) return rc;
-  std::vector<ResultCopy> h(nr);
-  for (size_t i = 0; i < nr; ++i) {
-    h[i] = ResultCopy{rs[i]->bits, rs[i]->changed, rs[i]->n_changed, p->snap + p->snap_bits[i],
-                      p->snap + p->snap_changed[i], p->d_counts + i, (uint32_t)((rs[i]->size_bits + 31) / 32), 0};
+  for (int s = 0; s < 2; ++s) CU(cudaMemsetAsync(p->cbuf[s], 0, (nr + 63) / 64 * 64 * 4, c->stream));
+  std::vector<ResultCopy> h(2 * nr);
+  for (int s = 0; s < 2; ++s)
+    for (size_t i = 0; i < nr; ++i)
+      h[s * nr + i] = ResultCopy{rs[i]->bits, rs[i]->changed, rs[i]->n_changed, p->cbuf[s] + p->snap_bits[i],
+                                 p->cbuf[s] + p->snap_changed[i], p->cbuf[s] + i,
+                                 (uint32_t)((rs[i]->size_bits + 31) / 32), 0};
+  if (nr) CU(cudaMemcpyAsync(p->d_copies, h.data(), 2 * nr * sizeof(ResultCopy), cudaMemcpyHostToDevice, c->stream));
+  // Launched view v culls result view_result[v] (the launched views are the jobs' views of
+  // non-empty groups, in job and view order).
+  p->view_result.assign(p->views.size(), -1);
+  size_t i = 0;
+  for (size_t v = 0; v < p->views.size(); ++v) {
+    while (i < nr && p->all_results[i] != p->results[v]) ++i;
+    if (i == nr) return fail(DPCULL_ERR_STATE, "plan views do not match its results");
+    p->view_result[v] = (int)i++;
   }
-  if (nr) CU(cudaMemcpyAsync(p->d_copies, h.data(), nr * sizeof(ResultCopy), cudaMemcpyHostToDevice, c->stream));
   if (!p->copy_stream) CU(cudaStreamCreateWithFlags(&p->copy_stream, cudaStreamNonBlocking));
   if (!p->snap_ev) CU(cudaEventCreateWithFlags(&p->snap_ev, cudaEventDisableTiming));
   if (!p->counts_ev) CU(cudaEventCreateWithFlags(&p->counts_ev, cudaEventDisableTiming));
-  if (!p->copies_ev) CU(cudaEventCreateWithFlags(&p->copies_ev, cudaEventDisableTiming));
+  for (int s = 0; s < 2; ++s)
+    if (!p->copies_ev[s]) CU(cudaEventCreateWithFlags(&p->copies_ev[s], cudaEventDisableTiming));
+  CU(cudaStreamSynchronize(c->stream));
+  p->copies = true;
   return DPCULL_OK;
+}
+
+// Points the slot's views at its copy buffer (on) or at nothing (off).  The slot's last
+// launch has finished (callers wait for it).
+static void plan_slot_copying(Plan* p, int s, bool on)
+{
+  if (p->copying[s] == on) return;
+  for (size_t v = 0; v < p->views.size(); ++v) {
+    CullView& cv = p->h_views[s][v];
+    const size_t i = (size_t)p->view_result[v];
+    cv.copy_bits = on ? p->cbuf[s] + p->snap_bits[i] : nullptr;
+    cv.copy_changed = on ? p->cbuf[s] + p->snap_changed[i] : nullptr;
+    cv.copy_count = on ? p->cbuf[s] + i : nullptr;
+  }
+  p->copying[s] = on;
 }
 
 // The results of a plan's launches, in job and view order (every one still alive).
@@ -1669,24 +1725,28 @@ int dpcull_plan_snapshot(dpcull_ctx c, dpcull_plan ph)
   if (!p) return fail(DPCULL_ERR_INVALID_ARGUMENT, "bad plan %u", ph);
   std::vector<Result*> rs;
   int rc = plan_results(c, ph, p, rs);
-  if (!rc) rc = plan_snapshot_setup(c, p, rs);
+  if (!rc) rc = plan_copies_setup(c, p, rs);
   if (rc) return rc;
   const size_t nr = rs.size();
-  // The snapshot overwrites what the previous read's copies are reading: wait for them
-  // on the device.
-  if (p->read_pending) CU(cudaStreamWaitEvent(c->stream, p->copies_ev, 0));
-  p->read_pending = false;
-  if (launch_snapshot(p->d_copies, (uint32_t)nr, p->snap_max_len, c->stream))
-    return cuda_fail(cudaGetLastError(), "snapshot launch");
-  c->launches++;
-  CU(cudaMemcpyAsync(p->d_counts + nr, &c->ctl->error, 2 * sizeof(unsigned int), cudaMemcpyDeviceToDevice,
-                     c->stream));
+  const int L = p->next ^ 1;  // the slot of the last launch
+  if (!p->copied[L]) {
+    // That launch did not write its copies (it came before the first asynchronous read,
+    // or ran while an earlier snapshot held the buffer): copy the live results, after the
+    // copies still reading the buffer.
+    if (p->read_pending[L]) CU(cudaStreamWaitEvent(c->stream, p->copies_ev[L], 0));
+    if (launch_snapshot(p->d_copies + (size_t)L * nr, (uint32_t)nr, p->snap_max_len, c->stream))
+      return cuda_fail(cudaGetLastError(), "snapshot launch");
+    c->launches++;
+    p->copied[L] = true;
+  }
   CU(cudaEventRecord(p->snap_ev, c->stream));
-  // The counts (and the error word) go to the host first: the list copies need their
-  // lengths.
+  // The counts and the error word go to the host first: the list copies need the lengths.
   CU(cudaStreamWaitEvent(p->copy_stream, p->snap_ev, 0));
-  CU(cudaMemcpyAsync(p->h_counts, p->d_counts, (nr + 2) * 4, cudaMemcpyDeviceToHost, p->copy_stream));
+  if (nr) CU(cudaMemcpyAsync(p->h_counts, p->cbuf[L], nr * 4, cudaMemcpyDeviceToHost, p->copy_stream));
+  CU(cudaMemcpyAsync(p->h_counts + nr, &c->ctl->error, 2 * sizeof(unsigned int), cudaMemcpyDeviceToHost,
+                     p->copy_stream));
   CU(cudaEventRecord(p->counts_ev, p->copy_stream));
+  p->snap_slot = L;
   p->snap_pending = true;
   return DPCULL_OK;
 }
@@ -1705,6 +1765,7 @@ int dpcull_plan_read_async(dpcull_ctx c, dpcull_plan ph, uint32_t* const* bits, 
     if (rc) return rc;
   }
   p->snap_pending = false;
+  const int L = p->snap_slot;
   const size_t nr = rs.size();
   CU(cudaEventSynchronize(p->counts_ev));
   if (p->h_counts[nr]) return check_device_errors(c);
@@ -1714,17 +1775,18 @@ int dpcull_plan_read_async(dpcull_ctx c, dpcull_plan ph, uint32_t* const* bits, 
     if (changed && changed[i] && cnt && (!changed_cap || cnt > changed_cap[i]))
       return fail(DPCULL_ERR_CAPACITY, "plan %u: result %zu has %u changed objects", ph, i, cnt);
   }
+  const uint32_t* buf = p->cbuf[L];
   for (size_t i = 0; i < nr; ++i) {
     const uint32_t cnt = p->h_counts[i];
     if (bits && bits[i] && p->snap_sizes[i])
-      CU(cudaMemcpyAsync(bits[i], p->snap + p->snap_bits[i], (p->snap_sizes[i] + 31) / 32 * 4,
-                         cudaMemcpyDeviceToHost, p->copy_stream));
+      CU(cudaMemcpyAsync(bits[i], buf + p->snap_bits[i], (p->snap_sizes[i] + 31) / 32 * 4, cudaMemcpyDeviceToHost,
+                         p->copy_stream));
     if (changed && changed[i] && cnt)
-      CU(cudaMemcpyAsync(changed[i], p->snap + p->snap_changed[i], (size_t)cnt * 4, cudaMemcpyDeviceToHost,
+      CU(cudaMemcpyAsync(changed[i], buf + p->snap_changed[i], (size_t)cnt * 4, cudaMemcpyDeviceToHost,
                          p->copy_stream));
   }
-  CU(cudaEventRecord(p->copies_ev, p->copy_stream));
-  p->read_pending = true;
+  CU(cudaEventRecord(p->copies_ev[L], p->copy_stream));
+  p->read_pending[L] = true;
   return DPCULL_OK;
 }
 
@@ -1732,8 +1794,10 @@ int dpcull_plan_read_wait(dpcull_ctx c, dpcull_plan ph)
 {
   Plan* p = get_plan(c, ph);
   if (!p) return fail(DPCULL_ERR_INVALID_ARGUMENT, "bad plan %u", ph);
-  if (p->read_pending) CU(cudaEventSynchronize(p->copies_ev));
-  p->read_pending = false;
+  for (int s = 0; s < 2; ++s) {
+    if (p->read_pending[s]) CU(cudaEventSynchronize(p->copies_ev[s]));
+    p->read_pending[s] = false;
+  }
   return DPCULL_OK;
 }
 
@@ -1764,10 +1828,11 @@ int dpcull_plan_destroy(dpcull_ctx c, dpcull_plan ph)
   if (p->copy_stream) cudaStreamDestroy(p->copy_stream);
   if (p->snap_ev) cudaEventDestroy(p->snap_ev);
   if (p->counts_ev) cudaEventDestroy(p->counts_ev);
-  if (p->copies_ev) cudaEventDestroy(p->copies_ev);
-  dfree(c, p->snap, p->snap_words * 4);
-  dfree(c, p->d_copies, std::max<size_t>(p->snap_sizes.size(), 1) * sizeof(ResultCopy));
-  dfree(c, p->d_counts, (p->snap_sizes.size() + 2) * 4);
+  for (int s = 0; s < 2; ++s) {
+    if (p->copies_ev[s]) cudaEventDestroy(p->copies_ev[s]);
+    dfree(c, p->cbuf[s], p->snap_words * 4);
+  }
+  dfree(c, p->d_copies, std::max<size_t>(2 * p->snap_sizes.size(), 1) * sizeof(ResultCopy));
   dfree(c, p->d_scenes, p->scenes.size() * sizeof(CullScene));
   dfree(c, p->d_views, p->views.size() * sizeof(CullView));
   *p = Plan();

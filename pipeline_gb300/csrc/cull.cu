@@ -517,6 +517,7 @@ __device__ __forceinline__ void finish_item(const WarpShared& ws, uint32_t tile_
         if (d) cv.bits[base + wd] = w;
         cv.delta[base + wd] = d;
       }
+      if (cv.copy_bits) cv.copy_bits[base + wd] = w;
     }
   }
   if (ws.cv[0].n_visible) {  // serving launches count every view's visible objects
@@ -732,7 +733,10 @@ __global__ void __launch_bounds__(kScanThreads)
   if (v.flags & kViewNoChanged) return;  // uniform
   const uint32_t w0 = blockIdx.x * kDeltaChunk;
   if (w0 >= v.n_words) {  // uniform
-    if (blockIdx.x == 0 && threadIdx.x == 0) *v.n_changed = 0;
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+      *v.n_changed = 0;
+      if (v.copy_count) *v.copy_count = 0;
+    }
     return;
   }
   // Changed objects of the earlier chunks.
@@ -741,7 +745,11 @@ __global__ void __launch_bounds__(kScanThreads)
   for (uint32_t i = threadIdx.x; i < blockIdx.x; i += kScanThreads) before += __ldcg(v.chunk_tot + i);
   block_scan(before, wsum, &tot);
   const uint32_t base = tot;
-  if (threadIdx.x == 0 && blockIdx.x == n_chunks - 1) *v.n_changed = base + __ldcg(v.chunk_tot + blockIdx.x);
+  if (threadIdx.x == 0 && blockIdx.x == n_chunks - 1) {
+    const uint32_t n = base + __ldcg(v.chunk_tot + blockIdx.x);
+    *v.n_changed = n;
+    if (v.copy_count) *v.copy_count = n;
+  }
   __syncthreads();  // tot is reused below
   const uint32_t b = w0 + threadIdx.x * kWordsPerThread;
   uint32_t w[kWordsPerThread];
@@ -755,7 +763,10 @@ __global__ void __launch_bounds__(kScanThreads)
     uint32_t m = w[j];
     while (m) {
       const int k = __ffs(m) - 1;
-      v.changed[pos++] = (b + (uint32_t)j) * 32u + (uint32_t)k;
+      const uint32_t obj = (b + (uint32_t)j) * 32u + (uint32_t)k;
+      v.changed[pos] = obj;
+      if (v.copy_changed) v.copy_changed[pos] = obj;
+      ++pos;
       m &= m - 1u;
     }
   }

@@ -135,7 +135,7 @@ inline uint32_t lay_out_items(CullScene* scenes, size_t n, uint32_t item_tiles, 
 // Single-tile units at the end of a launch: about two per warp that can be resident.
 inline uint64_t tail_units(int sm_count) { return (uint64_t)(sm_count > 0 ? sm_count : 1) * 64u; }
 
-struct alignas(16) CullView {   // 128 bytes; staged whole into shared memory by the cull
+struct alignas(16) CullView {   // 144 bytes; staged whole into shared memory by the cull
   float vp[16];
   uint32_t* bits;        // previous visibility on entry, new visibility on exit
   uint32_t* changed;     // ascending changed-object list
@@ -145,8 +145,13 @@ struct alignas(16) CullView {   // 128 bytes; staged whole into shared memory by
   uint32_t n_words;      // visibility words of the view (whole tiles)
   uint32_t flags;        // kViewNoChanged: write the visibility words only
   uint32_t* n_visible;   // optional: number of visible objects (accumulated)
+  // Optional second copies of the results (a plan's asynchronous reads): every new word,
+  // the changed list and its length, written beside bits / changed / n_changed.
+  uint32_t* copy_bits;
+  uint32_t* copy_changed;
+  uint32_t* copy_count;
 };
-static_assert(sizeof(CullView) == 128, "CullView is 128 bytes");
+static_assert(sizeof(CullView) == 144, "CullView is 144 bytes");
 
 // CullView::flags: no previous visibility and no changed list (bits are overwritten;
 // changed / n_changed / delta / chunk_tot are not used).

@@ -336,6 +336,64 @@ def test_plan_read_between_snapshot_and_async_read(ctx):
     ctx.group_destroy(g)
 
 
+def test_plan_snapshot_held_across_launches(ctx):
+    """Launches write their results into their slot's copy buffer once asynchronous reads
+    are in use.  A snapshot that is still unread when its slot is launched again keeps its
+    buffer (that launch skips its copies), a snapshot of a launch without copies copies the
+    live results, and every read returns the frame it snapshotted, against the port."""
+    n, nv = 70_001, 3
+    sc = W.stress_scene(seed=21, n_objects=n, n_transforms=3000)
+    g = setup_group(ctx, sc["lower"], sc["upper"], sc["xform"], sc["mats"])
+    rs = [ctx.result_create(g) for _ in range(nv)]
+    p = ctx.plan_create([(g, rs, sc["vps"][:nv])], dict(views_per_pass=4, tiles_per_ticket=1, ctas_per_sm=0))
+    rng = np.random.default_rng(22)
+    frames = [np.stack([W.jitter_view(rng, v, 20.0) for v in sc["vps"][:nv]]) for _ in range(6)]
+    obbs = oracle.build_obbs(sc["lower"], sc["extent"], sc["xform"], sc["mats"])
+    prev = [np.full((n + 31) // 32, 0xFFFFFFFF, np.uint32) for _ in range(nv)]
+    for w in prev:
+        w[-1] = (1 << (n % 32)) - 1
+    expect = []
+    for vps in frames:
+        fr = []
+        for v in range(nv):
+            bits = oracle.cull_obbs(obbs, vps[v], threads=8)
+            fr.append((bits, oracle.update_changed(prev[v], bits, n)))
+        expect.append(fr)
+
+    def launch(k):
+        ctx.plan_set_views(p, frames[k])
+        ctx.plan_launch(p)
+
+    def read_and_check(k):
+        bits = [np.zeros((n + 31) // 32, np.uint32) for _ in range(nv)]
+        ch = [np.zeros(n, np.uint32) for _ in range(nv)]
+        cnt = ctx.plan_read_async(p, bits, ch)
+        ctx.plan_read_wait(p)
+        for v in range(nv):
+            eb, ec = expect[k][v]
+            assert np.array_equal(bits[v], eb), (k, v)
+            assert cnt[v] == len(ec) and np.array_equal(ch[v][: len(ec)], ec), (k, v)
+
+    launch(0)
+    ctx.plan_snapshot(p)        # frame 0 was launched without copies: copied from the results
+    launch(1)                   # writes its copies
+    read_and_check(0)
+    ctx.plan_snapshot(p)        # frame 1, from its copies
+    launch(2)
+    launch(3)                   # the slot of the unread snapshot: no copies this time
+    read_and_check(1)
+    ctx.plan_snapshot(p)        # frame 3 has no copies: copied from the results
+    read_and_check(3)
+    launch(4)
+    read_and_check(4)           # no pending snapshot: one of the last launch
+    ctx.plan_snapshot(p)
+    launch(5)
+    read_and_check(4)
+    read_and_check(5)
+    ctx.plan_destroy(p)
+    ctx.group_destroy(g)
+
+
 def test_plan_autotuned(ctx, tmp_path, monkeypatch):
     sc = W.stress_scene(seed=10, n_objects=200_000, n_transforms=5000)
     g = setup_group(ctx, sc["lower"], sc["upper"], sc["xform"], sc["mats"])
