@@ -347,13 +347,13 @@ int dpcull_server_get_stats(dpcull_server s, dpcull_server_stats* out);
  *   changed   device, n entries: the ascending list of objects whose bit changed;
  *   n_changed device, one word: its length
  * The first call on a device looks up the scratch array's address with that device
- * current and keeps it until the process exits; make that first call before any stream
- * capture, and do not call this entry point on a device again after cudaDeviceReset of
- * that device (the reset destroys the array).  Every call shares the array (it keeps the
- * last call's contents; each call clears what must start at zero), so calls whose work
- * overlaps on the GPU race.  Waits for its work on `stream` (cudaStreamSynchronize) and
- * returns after it has finished; DPCULL_ERR_OUT_OF_RANGE if a transform index is past the
- * matrix array (those objects are left invisible). */
+ * current and keeps it until the process exits; do not call this entry point on a device
+ * again after cudaDeviceReset of that device (the reset destroys the array).  Every call
+ * shares the array (it keeps the last call's contents; each call clears what must start
+ * at zero), so calls whose work overlaps on the GPU race.  Blocks: waits for its work on
+ * `stream` (cudaStreamSynchronize) and returns after it has finished, so it cannot be
+ * called inside a stream capture; DPCULL_ERR_OUT_OF_RANGE if a transform index is past
+ * the matrix array (those objects are left invisible). */
 #define DPCULL_NOALLOC_MAX_OBJECTS (1u << 20)
 int dpcull_cull_noalloc(const float* objects, size_t cap, size_t n, const float* matrices,
                         size_t n_matrices, const float vp[16], uint32_t* bits, uint32_t* changed,

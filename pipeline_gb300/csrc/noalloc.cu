@@ -13,8 +13,9 @@
 //
 // The array lives in every GPU that loads this library until the process exits
 // (about 128 KB).  Its device address is looked up once per device, with that device
-// current, on the first call made on the device, and kept for the life of the process;
-// make that first call before any stream capture.  cudaDeviceReset destroys the array
+// current, on the first call made on the device, and kept for the life of the process.
+// Every call blocks until its work is done (cudaStreamSynchronize, then a copy to host
+// memory), so no call can be made inside a stream capture.  cudaDeviceReset destroys the array
 // together with the device's context, so after a reset of a device this entry point
 // must not be called on it again in the same process (the kept address would name
 // memory of the old context).  All calls share the array and it keeps the last call's
