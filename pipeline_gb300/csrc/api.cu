@@ -362,12 +362,14 @@ int result_prepare(dpcull_ctx c, Result& r, Group& g)
     r.bits = nb;
     CU(cudaStreamSynchronize(c->stream));
     dfree(c, r.delta, r.words_cap * 4);
-    dfree(c, r.chunk_tot, chunks_of(r.words_cap) * 4);
+    dfree(c, r.chunk_tot, (chunks_of(r.words_cap) + 2) * 4);
     r.delta = r.chunk_tot = nullptr;
     r.words_cap = words;
     rc = dalloc(c, (void**)&r.delta, words * 4);
-    if (!rc) rc = dalloc(c, (void**)&r.chunk_tot, chunks_of(words) * 4);
+    // the chunk counts, ticket and block count of the changed-list pass: zero between launches
+    if (!rc) rc = dalloc(c, (void**)&r.chunk_tot, (chunks_of(words) + 2) * 4);
     if (rc) return rc;
+    CU(cudaMemsetAsync(r.chunk_tot, 0, (chunks_of(words) + 2) * 4, c->stream));
   }
   const size_t chcap = std::max<size_t>(g.n, 1);
   if (chcap > r.changed_cap) {
@@ -504,6 +506,8 @@ int device_errors_read(dpcull_ctx c)
       return fail(DPCULL_ERR_OUT_OF_RANGE, "object %u has a transform index past the matrix array", info);
     if (err & kErrMisaligned)
       return fail(DPCULL_ERR_STATE, "work item %u: a matrix array moved off its 32-byte alignment", info);
+    if (err & kErrWaitTimeout)
+      return fail(DPCULL_ERR_CUDA, "changed-list assembly: a chunk count never arrived (results incomplete)");
   }
   return DPCULL_OK;
 }
@@ -650,9 +654,9 @@ int launch_batch(dpcull_ctx c, const CullScene* d_scenes, const CullView* d_view
   if (launch_cull(a, grid, (int)t.views_per_pass, s)) return cuda_fail(cudaGetLastError(), "cull launch");
   if (k1) CU(cudaEventRecordWithFlags(k1, s, cudaEventRecordExternal));
   CullView none{};
-  if (launch_changed_lists(d_views, none, n_views, max_words, s))
+  if (launch_changed_lists(d_views, none, n_views, max_words, &c->ctl->error, s))
     return cuda_fail(cudaGetLastError(), "changed-list launch");
-  c->launches += 3;
+  c->launches += 2;
   return DPCULL_OK;
 }
 
@@ -1130,7 +1134,7 @@ int dpcull_result_destroy(dpcull_ctx c, dpcull_result rh)
   dfree(c, r->changed, r->changed_cap * 4);
   dfree(c, r->n_changed, 4);
   dfree(c, r->delta, r->words_cap * 4);
-  dfree(c, r->chunk_tot, chunks_of(r->words_cap) * 4);
+  dfree(c, r->chunk_tot, (chunks_of(r->words_cap) + 2) * 4);
   if (r->group < c->groups.size()) {
     auto& v = c->groups[r->group].results;
     v.erase(std::remove(v.begin(), v.end(), rh), v.end());
@@ -1171,9 +1175,9 @@ int dpcull_cull(dpcull_ctx c, dpcull_group gh, dpcull_result rh, const float vp[
   a.n_items = lay_out_items(&a.one_scene, 1, a.item_tiles, tail_units(c->sm_count));
   const int grid = persistent_grid(c, 1, 0, a.n_items, 1, mode);
   if (launch_cull(a, grid, 1, c->stream)) return cuda_fail(cudaGetLastError(), "cull launch");
-  if (launch_changed_lists(nullptr, a.one_view, 1, a.one_view.n_words, c->stream))
+  if (launch_changed_lists(nullptr, a.one_view, 1, a.one_view.n_words, &c->ctl->error, c->stream))
     return cuda_fail(cudaGetLastError(), "changed-list launch");
-  c->launches += 3;
+  c->launches += 2;
   note_launch(c, groups, scenes, mode);
   return DPCULL_OK;
 }
@@ -1567,7 +1571,7 @@ int dpcull_plan_launch(dpcull_ctx c, dpcull_plan ph)
   note_launch(c, p->groups, p->scenes, mode);
   p->pending[s] = true;
   p->next ^= 1;
-  c->launches += 3;  // the graph's kernels: cull, chunk counts, changed-list emission
+  c->launches += 2;  // the graph's kernels: cull, changed lists
   return DPCULL_OK;
 }
 

@@ -19,7 +19,7 @@
 //      and set the visible ones in the words;
 //   4. per view of the item: XOR with the result's previous words (ResultBitSet::
 //      updateChanged), store the new words where they changed and the delta words.
-// No warp waits for another.  Two small kernels then turn the delta words into the packed
+// No warp waits for another.  One small kernel then turns the delta words into the packed
 // ascending changed list (launch_changed_lists).
 #include <algorithm>
 
@@ -668,12 +668,14 @@ __global__ void __launch_bounds__(kThreads, MODE == kCacheRead ? 4 : 3) cull_ker
 
 // ---- changed-list assembly ----------------------------------------------------------------
 // The delta words are grouped in chunks of kDeltaChunk (one block, 16 words per thread).
-// delta_totals_kernel counts each chunk's changed objects; emit_changed_kernel adds the
-// earlier chunks' counts and writes every changed index, ascending.  No block waits on
-// another.
+// One pass: the blocks of a view take its chunks in the order they start (a ticket), count
+// their chunk's changed objects and publish the count, then add the earlier chunks' counts
+// (published by blocks that started before them, so the wait always ends) and write every
+// changed index, ascending.  The view's last block clears the counts for the next launch.
 constexpr int kScanThreads = 256;
 constexpr int kWordsPerThread = kDeltaChunk / kScanThreads;
 static_assert(kWordsPerThread % 4 == 0, "whole uint4 loads");
+constexpr uint32_t kSpinLimit = 1u << 20;  // polls of an earlier chunk's count (~0.1 s)
 
 // The thread's delta words (n_words is a multiple of 4, the arrays 16-byte aligned).
 __device__ __forceinline__ void load_delta(const CullView& v, uint32_t b, uint32_t (&w)[kWordsPerThread])
@@ -708,56 +710,74 @@ __device__ __forceinline__ uint32_t block_scan(uint32_t x, uint32_t* wsum, uint3
 
 // grid = (chunks, views)
 __global__ void __launch_bounds__(kScanThreads)
-    delta_totals_kernel(const CullView* views, const __grid_constant__ CullView one)
+    emit_changed_kernel(const CullView* views, const __grid_constant__ CullView one, unsigned int* err)
 {
   __shared__ uint32_t wsum[kScanThreads / 32];
   __shared__ uint32_t tot;
-  const CullView& v = views ? views[blockIdx.y] : one;
-  if ((v.flags & kViewNoChanged) || blockIdx.x * kDeltaChunk >= v.n_words) return;  // uniform
-  uint32_t w[kWordsPerThread];
-  load_delta(v, blockIdx.x * kDeltaChunk + threadIdx.x * kWordsPerThread, w);
-  uint32_t s = 0;
-#pragma unroll
-  for (int j = 0; j < kWordsPerThread; ++j) s += (uint32_t)__popc(w[j]);
-  block_scan(s, wsum, &tot);
-  if (threadIdx.x == 0) v.chunk_tot[blockIdx.x] = tot;
-}
-
-// grid = (chunks, views)
-__global__ void __launch_bounds__(kScanThreads)
-    emit_changed_kernel(const CullView* views, const __grid_constant__ CullView one)
-{
-  __shared__ uint32_t wsum[kScanThreads / 32];
-  __shared__ uint32_t tot;
+  __shared__ uint32_t chunk;
+  __shared__ bool last;
   const CullView& v = views ? views[blockIdx.y] : one;
   if (v.flags & kViewNoChanged) return;  // uniform
-  const uint32_t w0 = blockIdx.x * kDeltaChunk;
-  if (w0 >= v.n_words) {  // uniform
+  const uint32_t n_chunks = (uint32_t)chunks_of(v.n_words);
+  if (blockIdx.x >= n_chunks) {  // uniform; only the view's first n_chunks blocks take tickets
     if (blockIdx.x == 0 && threadIdx.x == 0) {
       *v.n_changed = 0;
       if (v.copy_count) *v.copy_count = 0;
     }
     return;
   }
-  // Changed objects of the earlier chunks.
-  const uint32_t n_chunks = (uint32_t)chunks_of(v.n_words);
-  uint32_t before = 0;
-  for (uint32_t i = threadIdx.x; i < blockIdx.x; i += kScanThreads) before += __ldcg(v.chunk_tot + i);
-  block_scan(before, wsum, &tot);
-  const uint32_t base = tot;
-  if (threadIdx.x == 0 && blockIdx.x == n_chunks - 1) {
-    const uint32_t n = base + __ldcg(v.chunk_tot + blockIdx.x);
-    *v.n_changed = n;
-    if (v.copy_count) *v.copy_count = n;
-  }
-  __syncthreads();  // tot is reused below
-  const uint32_t b = w0 + threadIdx.x * kWordsPerThread;
+  uint32_t* state = v.chunk_tot;  // per chunk: its count + 1 once published
+  uint32_t* ticket = state + n_chunks;
+  uint32_t* done = ticket + 1;
+  if (threadIdx.x == 0) chunk = atomicAdd(ticket, 1u);
+  __syncthreads();
+  const uint32_t c = chunk;
+  const uint32_t b = c * kDeltaChunk + threadIdx.x * kWordsPerThread;
   uint32_t w[kWordsPerThread];
   load_delta(v, b, w);
   uint32_t s = 0;
 #pragma unroll
   for (int j = 0; j < kWordsPerThread; ++j) s += (uint32_t)__popc(w[j]);
-  uint32_t pos = base + block_scan(s, wsum, &tot);
+  const uint32_t in_block = block_scan(s, wsum, &tot);
+  const uint32_t count = tot;
+  if (threadIdx.x == 0) atomicExch(state + c, count + 1u);
+  // Changed objects of the earlier chunks: their blocks took earlier tickets, so they are
+  // running or done and publish without waiting for anything.
+  uint32_t before = 0;
+  bool gave_up = false;
+  for (uint32_t i = threadIdx.x; i < c; i += kScanThreads) {
+    uint32_t x = *(volatile const uint32_t*)(state + i);
+    for (uint32_t spins = 0; x == 0u; ++spins) {
+      if (spins == kSpinLimit) {
+        gave_up = true;
+        x = 1u;
+        break;
+      }
+      __nanosleep(64);
+      x = *(volatile const uint32_t*)(state + i);
+    }
+    before += x - 1u;
+  }
+  if (gave_up) atomicOr(err, kErrWaitTimeout);
+  __syncthreads();  // every thread has read tot
+  block_scan(before, wsum, &tot);
+  const uint32_t base = tot;
+  if (threadIdx.x == 0 && c == n_chunks - 1) {
+    const uint32_t n = base + count;
+    *v.n_changed = n;
+    if (v.copy_count) *v.copy_count = n;
+  }
+  // The last block past its reads clears the counts, the ticket and the block count.
+  if (threadIdx.x == 0) last = atomicAdd(done, 1u) == n_chunks - 1;
+  __syncthreads();
+  if (last) {
+    for (uint32_t i = threadIdx.x; i < n_chunks; i += kScanThreads) state[i] = 0u;
+    if (threadIdx.x == 0) {
+      *ticket = 0u;
+      *done = 0u;
+    }
+  }
+  uint32_t pos = base + in_block;
 #pragma unroll
   for (int j = 0; j < kWordsPerThread; ++j) {
     uint32_t m = w[j];
@@ -872,13 +892,12 @@ int cull_max_ctas_per_sm(int vpp, uint32_t mode)
 }
 
 int launch_changed_lists(const CullView* views, const CullView& one, uint32_t n_views,
-                         uint32_t max_words, void* stream)
+                         uint32_t max_words, unsigned int* err, void* stream)
 {
   cudaStream_t s = static_cast<cudaStream_t>(stream);
   if (!n_views) return 0;
   const uint32_t chunks = std::max<uint32_t>(1, (uint32_t)chunks_of(max_words));
-  delta_totals_kernel<<<dim3(chunks, n_views), kScanThreads, 0, s>>>(views, one);
-  emit_changed_kernel<<<dim3(chunks, n_views), kScanThreads, 0, s>>>(views, one);
+  emit_changed_kernel<<<dim3(chunks, n_views), kScanThreads, 0, s>>>(views, one, err);
   return cudaGetLastError() == cudaSuccess ? 0 : -1;
 }
 

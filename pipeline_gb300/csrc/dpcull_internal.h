@@ -71,6 +71,7 @@ DPCULL_HD_CONST size_t chunks_of(size_t n_words) { return (n_words + kDeltaChunk
 // Error bits reported through CullControl::error.
 constexpr uint32_t kErrBadTransform = 1u;   // transform index >= matrix count
 constexpr uint32_t kErrMisaligned = 2u;     // a wide launch met a matrix array not 32-byte aligned
+constexpr uint32_t kErrWaitTimeout = 4u;    // a changed-list block gave up waiting for an earlier count
 
 // Box cache of a group (the counterpart of the reference's OBB cache, GroupCPU::updateOBBs,
 // dp/culling/cpu/src/ManagerImpl.cpp:114-162): per object the prefilter box of
@@ -141,7 +142,9 @@ struct alignas(16) CullView {   // 144 bytes; staged whole into shared memory by
   uint32_t* changed;     // ascending changed-object list
   uint32_t* n_changed;   // its length
   uint32_t* delta;       // scratch: old XOR new visibility, n_words words
-  uint32_t* chunk_tot;   // scratch: changed objects per chunk of kDeltaChunk delta words
+  uint32_t* chunk_tot;   // scratch, zero between launches: per chunk of kDeltaChunk delta
+                        // words its changed objects + 1 once counted, then a ticket and a
+                        // block count (chunks_of(n_words) + 2 words)
   uint32_t n_words;      // visibility words of the view (whole tiles)
   uint32_t flags;        // kViewNoChanged: write the visibility words only
   uint32_t* n_visible;   // optional: number of visible objects (accumulated)
@@ -185,11 +188,12 @@ int launch_cull(const CullLaunch& args, int grid, int vpp, void* stream);
 // CTAs of the cull kernel of this kind (CacheMode) that fit on one SM.
 int cull_max_ctas_per_sm(int vpp, uint32_t mode);
 // Changed-list assembly after a cull launch over `n_views` views (device array `views`,
-// or the single `one` when views is null): per-chunk counts of the delta words, then the
-// emission of every changed index into the packed ascending list.  max_words bounds
-// n_words.
+// or the single `one` when views is null): one pass over the delta words that counts each
+// chunk, sums the earlier chunks' counts and emits every changed index into the packed
+// ascending list.  max_words bounds n_words; a block that gives up waiting for an earlier
+// chunk's count sets kErrWaitTimeout in *err.
 int launch_changed_lists(const CullView* views, const CullView& one, uint32_t n_views,
-                         uint32_t max_words, void* stream);
+                         uint32_t max_words, unsigned int* err, void* stream);
 
 // Transform propagation (xform.cu).
 struct XformLaunch {

@@ -38,7 +38,7 @@ namespace {
 constexpr size_t kNoallocWords = DPCULL_NOALLOC_MAX_OBJECTS / 32;
 constexpr size_t kDeltaBytes = kNoallocWords * sizeof(uint32_t);
 constexpr size_t kChunkOffset = kDeltaBytes;
-constexpr size_t kCtlOffset = kChunkOffset + (chunks_of(kNoallocWords) * sizeof(uint32_t) + 255) / 256 * 256;
+constexpr size_t kCtlOffset = kChunkOffset + ((chunks_of(kNoallocWords) + 2) * sizeof(uint32_t) + 255) / 256 * 256;
 constexpr size_t kScratchBytes = kCtlOffset + 256;
 static_assert(DPCULL_NOALLOC_MAX_OBJECTS % kTileObjects == 0, "whole tiles");
 
@@ -95,8 +95,9 @@ extern "C" int dpcull_cull_noalloc(const float* objects, size_t cap, size_t n, c
     return noalloc_fail(DPCULL_ERR_CUDA, "dpcull_cull_noalloc: cudaGetSymbolAddress failed");
   cudaStream_t st = static_cast<cudaStream_t>(stream);
   CullControl* ctl = reinterpret_cast<CullControl*>(s + kCtlOffset);
-  // The ticket, CTA counter and error word must start at zero.
-  if (cudaMemsetAsync(ctl, 0, sizeof(CullControl), st) != cudaSuccess) {
+  // The changed-list pass's counts, the ticket, CTA counter and error word must start at
+  // zero (the counts end every call at zero; cleared here all the same).
+  if (cudaMemsetAsync(s + kChunkOffset, 0, kCtlOffset - kChunkOffset + sizeof(CullControl), st) != cudaSuccess) {
     cudaGetLastError();
     return noalloc_fail(DPCULL_ERR_CUDA, "dpcull_cull_noalloc: cudaMemsetAsync failed");
   }
@@ -132,7 +133,7 @@ extern "C" int dpcull_cull_noalloc(const float* objects, size_t cap, size_t n, c
   a.item_tiles = item_tiles_for(tiles, sms);
   a.n_items = lay_out_items(&a.one_scene, 1, a.item_tiles, tail_units(sms));
   const int grid = (int)((a.n_items + kWarpsPerCta - 1) / kWarpsPerCta);  // one item per warp
-  if (launch_cull(a, grid, 1, st) || launch_changed_lists(nullptr, a.one_view, 1, a.one_view.n_words, st)) {
+  if (launch_cull(a, grid, 1, st) || launch_changed_lists(nullptr, a.one_view, 1, a.one_view.n_words, &ctl->error, st)) {
     cudaGetLastError();
     return noalloc_fail(DPCULL_ERR_CUDA, "dpcull_cull_noalloc: launch failed");
   }
@@ -144,6 +145,8 @@ extern "C" int dpcull_cull_noalloc(const float* objects, size_t cap, size_t n, c
     cudaGetLastError();
     return noalloc_fail(DPCULL_ERR_CUDA, "dpcull_cull_noalloc: the cull failed on the device");
   }
+  if (err[0] & kErrWaitTimeout)
+    return noalloc_fail(DPCULL_ERR_CUDA, "dpcull_cull_noalloc: changed-list assembly incomplete");
   if (err[0] & kErrBadTransform)
     return noalloc_fail(DPCULL_ERR_OUT_OF_RANGE, "dpcull_cull_noalloc: a transform index is past the matrix array");
   return DPCULL_OK;
