@@ -9,9 +9,9 @@
 // A result (one group x one view) owns its visibility bit array (bit i of word i/32 is
 // object i, the ResultBitSet layout, padded to whole tiles), its changed-object list and
 // its scratch: the delta words (bit i set where object i changed; the cull writes every
-// word) and one changed count per chunk of kDeltaChunk delta words.  Two small kernels
-// turn the delta words into the packed ascending list.  A tile is the 128 objects of one
-// warp.
+// word) and one changed count per chunk of kDeltaChunk delta words (with a ticket and a
+// block count).  One small kernel, a single pass, turns the delta words into the packed
+// ascending list.  A tile is the 128 objects of one warp.
 #pragma once
 
 #include <cstddef>
