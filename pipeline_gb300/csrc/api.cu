@@ -1644,7 +1644,7 @@ static int plan_copies_setup(dpcull_ctx c, Plan* p, const std::vector<Result*>& 
       p->h_views[s][v].copy_bits = p->h_views[s][v].copy_changed = p->h_views[s][v].copy_count = nullptr;
     }
   }
-  dfree(c, p->d_copies, p->snap_sizes.size() * 2 * sizeof(ResultCopy));
+  dfree(c, p->d_copies, std::max<size_t>(2 * p->snap_sizes.size(), 1) * sizeof(ResultCopy));
   p->d_copies = nullptr;
   p->copies = false;
   p->snap_pending = false;
