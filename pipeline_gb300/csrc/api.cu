@@ -648,15 +648,16 @@ int launch_batch(dpcull_ctx c, const CullScene* d_scenes, const CullView* d_view
   a.items_per_ticket = std::max<uint32_t>(1, t.tiles_per_ticket);
   a.exact_only = c->exact_only ? 1u : 0u;
   a.cache_mode = mode;
+  a.emit_views = fused_emit_views(n_views, max_words);
   a.ctl = c->ctl;
   const int grid = persistent_grid(c, t.views_per_pass, t.ctas_per_sm, n_items, a.items_per_ticket, mode);
   if (k0) CU(cudaEventRecordWithFlags(k0, s, cudaEventRecordExternal));
   if (launch_cull(a, grid, (int)t.views_per_pass, s)) return cuda_fail(cudaGetLastError(), "cull launch");
   if (k1) CU(cudaEventRecordWithFlags(k1, s, cudaEventRecordExternal));
   CullView none{};
-  if (launch_changed_lists(d_views, none, n_views, max_words, &c->ctl->error, s))
+  if (!a.emit_views && launch_changed_lists(d_views, none, n_views, max_words, &c->ctl->error, s))
     return cuda_fail(cudaGetLastError(), "changed-list launch");
-  c->launches += 2;
+  c->launches += a.emit_views ? 1 : 2;
   return DPCULL_OK;
 }
 
@@ -1173,11 +1174,12 @@ int dpcull_cull(dpcull_ctx c, dpcull_group gh, dpcull_result rh, const float vp[
   a.one_view = view_of(*r, vp);
   a.item_tiles = item_tiles_for(a.one_scene.n_tiles, c->sm_count);
   a.n_items = lay_out_items(&a.one_scene, 1, a.item_tiles, tail_units(c->sm_count));
+  a.emit_views = fused_emit_views(1, a.one_view.n_words);
   const int grid = persistent_grid(c, 1, 0, a.n_items, 1, mode);
   if (launch_cull(a, grid, 1, c->stream)) return cuda_fail(cudaGetLastError(), "cull launch");
-  if (launch_changed_lists(nullptr, a.one_view, 1, a.one_view.n_words, &c->ctl->error, c->stream))
+  if (!a.emit_views && launch_changed_lists(nullptr, a.one_view, 1, a.one_view.n_words, &c->ctl->error, c->stream))
     return cuda_fail(cudaGetLastError(), "changed-list launch");
-  c->launches += 2;
+  c->launches += a.emit_views ? 1 : 2;
   note_launch(c, groups, scenes, mode);
   return DPCULL_OK;
 }
@@ -1571,7 +1573,8 @@ int dpcull_plan_launch(dpcull_ctx c, dpcull_plan ph)
   note_launch(c, p->groups, p->scenes, mode);
   p->pending[s] = true;
   p->next ^= 1;
-  c->launches += 2;  // the graph's kernels: cull, changed lists
+  // the graph's kernels: the cull, and the changed lists unless the cull builds them
+  c->launches += fused_emit_views((uint32_t)p->views.size(), max_words_of(p->scenes)) ? 1 : 2;
   return DPCULL_OK;
 }
 

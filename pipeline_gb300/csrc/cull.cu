@@ -613,6 +613,10 @@ __device__ __forceinline__ void warp_item(const CullLaunch& a, uint32_t item, Wa
   finish_item<VPP>(ws, tile_first, n_t, nv, lane);
 }
 
+// The changed list of a view whose delta words fit one chunk, by one CTA (defined with the
+// changed-list assembly below).
+__device__ void emit_small_view(const CullView& v);
+
 // The kernels that transform the boxes hold 80 registers (3 CTAs of 256 threads per SM);
 // the one that reads the box cache needs fewer and runs at 4.
 template <int VPP, bool PF, bool WIDE, uint32_t MODE>
@@ -663,6 +667,9 @@ __global__ void __launch_bounds__(kThreads, MODE == kCacheRead ? 4 : 3) cull_ker
       ctl->ticket = 0;
       ctl->done = 0;
     }
+    // Small launches: the changed lists too (every CTA's delta words are visible: each
+    // fenced its stores before counting itself done).
+    for (uint32_t v = 0; v < a.emit_views; ++v) emit_small_view(a.views ? a.views[v] : a.one_view);
   }
 }
 
@@ -790,6 +797,40 @@ __global__ void __launch_bounds__(kScanThreads)
       m &= m - 1u;
     }
   }
+}
+
+// One view's changed list from its delta words, all in one chunk: chunk count and block
+// scan in one block (the cull kernel's last CTA, kScanThreads threads).
+static_assert(kThreads == kScanThreads, "the cull kernel's CTA runs the block scan");
+__device__ void emit_small_view(const CullView& v)
+{
+  __shared__ uint32_t wsum[kScanThreads / 32];
+  __shared__ uint32_t tot;
+  if (v.flags & kViewNoChanged) return;  // uniform
+  const uint32_t b = threadIdx.x * kWordsPerThread;
+  uint32_t w[kWordsPerThread];
+  load_delta(v, b, w);
+  uint32_t s = 0;
+#pragma unroll
+  for (int j = 0; j < kWordsPerThread; ++j) s += (uint32_t)__popc(w[j]);
+  uint32_t pos = block_scan(s, wsum, &tot);
+  if (threadIdx.x == 0) {
+    *v.n_changed = tot;
+    if (v.copy_count) *v.copy_count = tot;
+  }
+#pragma unroll
+  for (int j = 0; j < kWordsPerThread; ++j) {
+    uint32_t m = w[j];
+    while (m) {
+      const int k = __ffs(m) - 1;
+      const uint32_t obj = (b + (uint32_t)j) * 32u + (uint32_t)k;
+      v.changed[pos] = obj;
+      if (v.copy_changed) v.copy_changed[pos] = obj;
+      ++pos;
+      m &= m - 1u;
+    }
+  }
+  __syncthreads();  // wsum and tot are used again for the next view
 }
 
 template <int VPP, bool WIDE>

@@ -178,6 +178,8 @@ struct CullLaunch {
   uint32_t wide_mats;        // 1 = every scene's matrix array is 32-byte aligned (256-bit
                              // matrix loads); set by launch_cull itself for `one_scene`
   uint32_t cache_mode;       // CacheMode: the fused, Fill or cached kernel (the host's choice)
+  uint32_t emit_views;       // > 0: every view's delta words fit one chunk, and the launch's
+                             // last CTA builds the changed lists of these views itself
   CullControl* ctl;
   CullScene one_scene;
   CullView one_view;
@@ -194,6 +196,13 @@ int cull_max_ctas_per_sm(int vpp, uint32_t mode);
 // chunk's count sets kErrWaitTimeout in *err.
 int launch_changed_lists(const CullView* views, const CullView& one, uint32_t n_views,
                          uint32_t max_words, unsigned int* err, void* stream);
+// Launches of at most this many views whose delta words fit one chunk build their changed
+// lists in the cull kernel's last CTA (CullLaunch::emit_views): no second kernel.
+constexpr uint32_t kFusedEmitViews = 4;
+inline uint32_t fused_emit_views(uint32_t n_views, uint32_t max_words)
+{
+  return (n_views <= kFusedEmitViews && max_words <= kDeltaChunk) ? n_views : 0u;
+}
 
 // Transform propagation (xform.cu).
 struct XformLaunch {

@@ -133,7 +133,9 @@ extern "C" int dpcull_cull_noalloc(const float* objects, size_t cap, size_t n, c
   a.item_tiles = item_tiles_for(tiles, sms);
   a.n_items = lay_out_items(&a.one_scene, 1, a.item_tiles, tail_units(sms));
   const int grid = (int)((a.n_items + kWarpsPerCta - 1) / kWarpsPerCta);  // one item per warp
-  if (launch_cull(a, grid, 1, st) || launch_changed_lists(nullptr, a.one_view, 1, a.one_view.n_words, &ctl->error, st)) {
+  a.emit_views = fused_emit_views(1, a.one_view.n_words);
+  if (launch_cull(a, grid, 1, st) ||
+      (!a.emit_views && launch_changed_lists(nullptr, a.one_view, 1, a.one_view.n_words, &ctl->error, st))) {
     cudaGetLastError();
     return noalloc_fail(DPCULL_ERR_CUDA, "dpcull_cull_noalloc: launch failed");
   }
