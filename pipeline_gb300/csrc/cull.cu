@@ -22,6 +22,7 @@
 // No warp waits for another.  One small kernel then turns the delta words into the packed
 // ascending changed list (launch_changed_lists).
 #include <algorithm>
+#include <atomic>
 
 #include <cuda_runtime.h>
 
@@ -853,14 +854,16 @@ int launch_vpp(const CullLaunch& a, int grid, cudaStream_t s)
 template <int VPP, uint32_t MODE>
 int max_ctas()
 {
-  static int cached = 0;  // the same for every GB300; a race only writes the same value
-  if (cached) return cached;
+  static std::atomic<int> cached{0};  // the same on every GB300: threads that race store the same value
+  const int known = cached.load(std::memory_order_relaxed);
+  if (known) return known;
   int n = 0;
   if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, cull_kernel<VPP, true, true, MODE>, kThreads, 0) !=
       cudaSuccess)
     return 1;
-  cached = n > 0 ? n : 1;
-  return cached;
+  n = n > 0 ? n : 1;
+  cached.store(n, std::memory_order_relaxed);
+  return n;
 }
 
 template <int VPP>
