@@ -268,17 +268,24 @@ void copy_kept(Slot& slot)
 
 // Starts the uploads of scenes that requests found missing (after the turn's batch went
 // out, so no hit waits on these calls).  At most half the budget is in uploads that no
-// batch has taken yet (any one scene may upload alone).
+// batch has taken yet (any one scene may upload alone), and at most kUploadsPerTurn start
+// per turn, so a burst of misses does not hold the scheduler from its next batch (the
+// requests of the others stay pending and ask again next turn).
+constexpr int kUploadsPerTurn = 8;
 void start_uploads(dpcull_server s, const std::vector<uint32_t>& missing)
 {
   if (missing.empty()) return;
   std::lock_guard<std::mutex> lk(s->scenes_mu);
+  int started = 0;
   for (uint32_t id : missing) {
+    if (started == kUploadsPerTurn) break;
     Scene& sc = s->scenes[id];
     if (sc.resident) continue;  // two requests of this turn wanted it
     if ((s->uploading_bytes == 0 || s->uploading_bytes + sc.bytes <= s->budget / 2) &&
-        make_room(s, sc.bytes, false))
+        make_room(s, sc.bytes, false)) {
       upload(s, sc, id);
+      ++started;
+    }
   }
 }
 
