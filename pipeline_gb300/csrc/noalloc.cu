@@ -6,10 +6,10 @@
 // entirely owned by another allocator (a framework's caching allocator, or a fixed
 // budget reserved up front) has none to give.  The regular entry points allocate their
 // result buffers and the cull's scratch lazily, so they are unusable there.  This entry
-// point runs the same cull kernel and the same changed-list kernels on buffers the
-// caller owns, and takes its scratch (the delta words of the changed list, their
-// per-chunk counts and the work-ticket word) from one statically sized device array
-// defined below.  It calls no cudaMalloc, cudaFree or other allocating routine.
+// point runs the same cull kernel and the same changed-list assembly on buffers the
+// caller owns, and takes its scratch (the delta words of the changed list, the changed-list
+// pass's per-chunk counts, ticket and block count, and the cull's control block) from one
+// statically sized device array defined below.  It calls no cudaMalloc, cudaFree or other allocating routine.
 //
 // The array lives in every GPU that loads this library until the process exits
 // (about 128 KB).  Its device address is looked up once per device, with that device
