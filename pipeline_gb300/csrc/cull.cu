@@ -627,6 +627,9 @@ __global__ void __launch_bounds__(kThreads, MODE == kCacheRead ? 4 : 3) cull_ker
   WarpShared& ws = wsh[threadIdx.x >> 5];
   const int lane = threadIdx.x & 31;
   CullControl* ctl = a.ctl;
+  // The changed-list kernel after this one may start launching once every CTA of this
+  // grid runs (it waits for this grid's completion before it reads anything).
+  asm volatile("griddepcontrol.launch_dependents;");
   if (threadIdx.x % 32 == 0) {
     ws.sc.item_begin = 0;  // no scene cached: the first item looks its scene up
     ws.sc.n_tiles = 0;
@@ -724,6 +727,8 @@ __global__ void __launch_bounds__(kScanThreads)
   __shared__ uint32_t tot;
   __shared__ uint32_t chunk;
   __shared__ bool last;
+  // Launched as a programmatic dependent of the cull: wait for its grid and its memory.
+  asm volatile("griddepcontrol.wait;" ::: "memory");
   const CullView& v = views ? views[blockIdx.y] : one;
   if (v.flags & kViewNoChanged) return;  // uniform
   const uint32_t n_chunks = (uint32_t)chunks_of(v.n_words);
@@ -941,7 +946,16 @@ int launch_changed_lists(const CullView* views, const CullView& one, uint32_t n_
   cudaStream_t s = static_cast<cudaStream_t>(stream);
   if (!n_views) return 0;
   const uint32_t chunks = std::max<uint32_t>(1, (uint32_t)chunks_of(max_words));
-  emit_changed_kernel<<<dim3(chunks, n_views), kScanThreads, 0, s>>>(views, one, err);
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3(chunks, n_views);
+  cfg.blockDim = dim3(kScanThreads);
+  cfg.stream = s;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  attr[0].val.programmaticStreamSerializationAllowed = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  if (cudaLaunchKernelEx(&cfg, emit_changed_kernel, views, one, err) != cudaSuccess) return -1;
   return cudaGetLastError() == cudaSuccess ? 0 : -1;
 }
 
