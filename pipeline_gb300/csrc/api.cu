@@ -256,7 +256,7 @@ int cache_stale(dpcull_ctx c, Group& g)
 {
   g.cache_launches = 0;
   g.cache_filled = false;
-  if (g.cache_state) CU(cudaMemsetAsync(g.cache_state, 0, sizeof(uint32_t), c->stream));
+  if (g.cache_state) CU(cudaMemsetAsync(g.cache_state, 0, kCacheStateBytes, c->stream));
   return DPCULL_OK;
 }
 
@@ -851,13 +851,13 @@ int dpcull_group_create(dpcull_ctx c, dpcull_group* out)
     return rc;
   }
   CU(cudaMemsetAsync(g.box_scratch, 0, (bbox_partials_needed(0) + 16) * sizeof(float), c->stream));
-  rc = dalloc(c, (void**)&g.cache_state, 16);
+  rc = dalloc(c, (void**)&g.cache_state, kCacheStateBytes);
   if (rc) {
     dfree(c, g.box_scratch, (bbox_partials_needed(0) + 16) * sizeof(float));
     g = Group();
     return rc;
   }
-  CU(cudaMemsetAsync(g.cache_state, 0, 16, c->stream));
+  CU(cudaMemsetAsync(g.cache_state, 0, kCacheStateBytes, c->stream));
   *out = (dpcull_group)(c->groups.size() - 1);
   return DPCULL_OK;
 }
@@ -871,7 +871,7 @@ int dpcull_group_destroy(dpcull_ctx c, dpcull_group gh)
     if (get_result(c, r)) dpcull_result_destroy(c, r);
   dfree(c, g->soa, soa_bytes(g->cap));
   dfree(c, g->cache, cache_bytes(g->cap));
-  dfree(c, g->cache_state, 16);
+  dfree(c, g->cache_state, kCacheStateBytes);
   if (g->mats_cap) dfree(c, g->mats, g->mats_cap * 64);
   dfree(c, g->box_scratch, (bbox_partials_needed(0) + 16) * sizeof(float));
   *g = Group();

@@ -64,6 +64,9 @@ struct WarpShared {
   uint32_t words[kMaxViewsPerPass][kItemTiles][kTileWords];  // the item's visibility words
   uint16_t queue[kQueueCap];                             // tile << 10 | object << 3 | view
   ulonglong2 qp[kMaxViewsPerPass][3][2];                 // per axis: (lo, hi) pairs of x, y | z, w
+  float4 zlo[kMaxViewsPerPass];                          // the z-lo planes alone (five-plane test)
+  uint32_t far_off;                                      // the group may leave out its z-hi planes
+  uint32_t bnd[kBoundWords];                             // Fill: the item's scene-bound keys
 };
 static_assert(kTileObjects == 32 * kObjPerThread, "a tile is one warp's objects");
 static_assert(kItemTiles * kTileWords <= 32, "one word of a view's item per lane");
@@ -213,6 +216,27 @@ __device__ __forceinline__ void decide_object(const unsigned long long (&cx)[kOb
   pf::decide_bits<1u << K>(xl, xh, yl, yh, zl, zh, D[K], nT[K], in, un);
 }
 
+// The same without the z-hi plane (the scene bound cleared it): the z-lo value alone, the
+// scalar FMA chain of the packed pair's lo half.
+template <int K>
+__device__ __forceinline__ void decide_object5(const unsigned long long (&cx)[kObjPerThread],
+                                               const unsigned long long (&cy)[kObjPerThread],
+                                               const unsigned long long (&cz)[kObjPerThread],
+                                               const ulonglong2& ax0, const ulonglong2& ax1,
+                                               const ulonglong2& ay0, const ulonglong2& ay1, const float4& zq,
+                                               const float (&D)[kObjPerThread], const float (&nT)[kObjPerThread],
+                                               uint32_t& in, uint32_t& un)
+{
+  float xl, xh, yl, yh, c0, c1, c2, dup;
+  upk2(fma2(cz[K], ax1.x, fma2(cy[K], ax0.y, fma2(cx[K], ax0.x, ax1.y))), xl, xh);
+  upk2(fma2(cz[K], ay1.x, fma2(cy[K], ay0.y, fma2(cx[K], ay0.x, ay1.y))), yl, yh);
+  upk2(cx[K], c0, dup);
+  upk2(cy[K], c1, dup);
+  upk2(cz[K], c2, dup);
+  const float zl = __fmaf_rn(c2, zq.z, __fmaf_rn(c1, zq.y, __fmaf_rn(c0, zq.x, zq.w)));
+  pf::decide_bits5<1u << K>(xl, xh, yl, yh, zl, D[K], nT[K], in, un);
+}
+
 // Prefilter of the lane's 4 boxes in each view of the item; returns the undecided pairs
 // (bit layout: und_object / und_view below).  With several views the visible bits collect
 // as nibbles (bit 4v + k: object k, view v) and one nibble transpose per tile gives every
@@ -223,8 +247,9 @@ __device__ __forceinline__ void decide_object(const unsigned long long (&cx)[kOb
 // box and view: 9 paired FMAs for the six plane values, then pf::decide_bits against the
 // view group's margin (each box's two thresholds are computed once for all the group's
 // views): one comparison and one predicated OR per bit.  Branch-free per pair; the view
-// loop is not unrolled (nv is uniform over the warp).
-template <int VPP>
+// loop is not unrolled (nv is uniform over the warp).  SIX = false: the five-plane test of
+// a group whose scene bound cleared every z-hi plane (the same bits: pf::far_plane_clear).
+template <int VPP, bool SIX = true>
 __device__ __forceinline__ uint32_t classify_views(WarpShared& ws, const pf::Box (&bx)[kObjPerThread],
                                                    int nv, uint32_t t, uint32_t valid, int lane)
 {
@@ -248,12 +273,20 @@ __device__ __forceinline__ uint32_t classify_views(WarpShared& ws, const pf::Box
   for (int v = nv - 1; v >= 0; --v) {
     const ulonglong2 ax0 = ws.qp[v][0][0], ax1 = ws.qp[v][0][1];
     const ulonglong2 ay0 = ws.qp[v][1][0], ay1 = ws.qp[v][1][1];
-    const ulonglong2 az0 = ws.qp[v][2][0], az1 = ws.qp[v][2][1];
     uint32_t in = VPP == 1 ? 0u : vis_n << 4, un = VPP == 1 ? 0u : und_n << 4;
-    decide_object<0>(cx, cy, cz, ax0, ax1, ay0, ay1, az0, az1, D, nT, in, un);
-    decide_object<1>(cx, cy, cz, ax0, ax1, ay0, ay1, az0, az1, D, nT, in, un);
-    decide_object<2>(cx, cy, cz, ax0, ax1, ay0, ay1, az0, az1, D, nT, in, un);
-    decide_object<3>(cx, cy, cz, ax0, ax1, ay0, ay1, az0, az1, D, nT, in, un);
+    if (SIX) {
+      const ulonglong2 az0 = ws.qp[v][2][0], az1 = ws.qp[v][2][1];
+      decide_object<0>(cx, cy, cz, ax0, ax1, ay0, ay1, az0, az1, D, nT, in, un);
+      decide_object<1>(cx, cy, cz, ax0, ax1, ay0, ay1, az0, az1, D, nT, in, un);
+      decide_object<2>(cx, cy, cz, ax0, ax1, ay0, ay1, az0, az1, D, nT, in, un);
+      decide_object<3>(cx, cy, cz, ax0, ax1, ay0, ay1, az0, az1, D, nT, in, un);
+    } else {
+      const float4 zq = ws.zlo[v];
+      decide_object5<0>(cx, cy, cz, ax0, ax1, ay0, ay1, zq, D, nT, in, un);
+      decide_object5<1>(cx, cy, cz, ax0, ax1, ay0, ay1, zq, D, nT, in, un);
+      decide_object5<2>(cx, cy, cz, ax0, ax1, ay0, ay1, zq, D, nT, in, un);
+      decide_object5<3>(cx, cy, cz, ax0, ax1, ay0, ay1, zq, D, nT, in, un);
+    }
     if (VPP == 1) {
       // bit k of un -> bit 8k (the multiply places each bit k at 8k; the mask drops the
       // cross terms); one view per pass, so v == 0
@@ -369,6 +402,33 @@ __device__ __forceinline__ void store_boxes(const CullScene& sc, uint32_t obj0, 
   __stcg(reinterpret_cast<float4*>(sc.box + 4 * cap + obj0), make_float4(bx[0].d0, bx[1].d0, bx[2].d0, bx[3].d0));
 }
 
+// Fill launches: the tile's boxes into the item's scene bound (the bound words of the
+// cache's state block, see pf::far_plane_clear): per lane over its boxes whose margin is a
+// number, then one warp reduction per word; lane 0 keeps the item's running maximum.
+__device__ __forceinline__ void gather_bound(WarpShared& ws, const pf::Box (&bx)[kObjPerThread], uint32_t valid,
+                                             int lane)
+{
+  uint32_t key[kBoundWords] = {0u, 0u, 0u, 0u, 0u, 0u, 0u};
+#pragma unroll
+  for (int k = 0; k < kObjPerThread; ++k) {
+    if (((valid >> k) & 1u) && bx[k].d0 == bx[k].d0) {
+      const uint32_t x = pf::bound_key(bx[k].cx), y = pf::bound_key(bx[k].cy), z = pf::bound_key(bx[k].cz);
+      key[0] = max(key[0], x);
+      key[1] = max(key[1], y);
+      key[2] = max(key[2], z);
+      key[3] = max(key[3], ~x);
+      key[4] = max(key[4], ~y);
+      key[5] = max(key[5], ~z);
+      key[6] = max(key[6], pf::bound_key(bx[k].d0));
+    }
+  }
+#pragma unroll
+  for (int w = 0; w < kBoundWords; ++w) {
+    const uint32_t m = __reduce_max_sync(0xffffffffu, key[w]);
+    if (lane == 0) ws.bnd[w] = max(ws.bnd[w], m);
+  }
+}
+
 // Classification of one tile into the item's words (visible objects) and queue
 // (undecided pairs).  Returns the new queue length.  WIDE: the scene's matrix array is
 // 32-byte aligned (two 256-bit loads per matrix).  MODE: the fused kernel computes the
@@ -396,7 +456,8 @@ __device__ __forceinline__ uint32_t classify_tile(const CullLaunch& a, WarpShare
         for (int r = 0; r < kBoxRows; ++r) asm volatile("prefetch.global.L1 [%0];" ::"l"(nb + r * cap));
       }
       const uint32_t valid = cached_boxes(sc, obj0, bx);
-      amb = classify_views<VPP>(ws, bx, nv, t, valid, lane);
+      amb = ws.far_off ? classify_views<VPP, false>(ws, bx, nv, t, valid, lane)
+                       : classify_views<VPP, true>(ws, bx, nv, t, valid, lane);
     } else {
       // A Stale cache (the host never launches this kernel on one): no visible bit from the
       // prefilter, every pair of the lane's objects to the exact test.
@@ -453,7 +514,10 @@ __device__ __forceinline__ uint32_t classify_tile(const CullLaunch& a, WarpShare
       const uint32_t o = obj0 + (uint32_t)__ffs(bad) - 1u;
       if (atomicOr(&a.ctl->error, kErrBadTransform) == 0) a.ctl->error_info = o;
     }
-    if (MODE == kCacheFill && sc.box) store_boxes(sc, obj0, bx);
+    if (MODE == kCacheFill && sc.box) {
+      store_boxes(sc, obj0, bx);
+      gather_bound(ws, bx, valid, lane);
+    }
     const uint32_t amb = classify_views<VPP>(ws, bx, nv, t, valid, lane);
     return push_undecided<VPP, MODE>(ws, sc, tile_first, t, qn, amb, lane, false);
   }
@@ -582,25 +646,47 @@ __device__ __forceinline__ void warp_item(const CullLaunch& a, uint32_t item, Wa
     __syncwarp();
     if (PF) {
       pf::GroupMargin m{0.f, 0.f};
+      pf::Planes pl;
       if (lane < nv) {
-        pf::Planes pl;
         pf::group_view(ws.cv[lane].vp, pl, m);
         for (int ax = 0; ax < 3; ++ax) {
           const pf::F4 lo = pl.q[ax][0], hi = pl.q[ax][1];
           ws.qp[lane][ax][0] = make_ulonglong2(pk2(lo.x, hi.x), pk2(lo.y, hi.y));
           ws.qp[lane][ax][1] = make_ulonglong2(pk2(lo.z, hi.z), pk2(lo.w, hi.w));
         }
+        if (MODE == kCacheRead) ws.zlo[lane] = make_float4(pl.q[2][0].x, pl.q[2][0].y, pl.q[2][0].z, pl.q[2][0].w);
       }
       // the group margin: the largest over the views (lanes past nv contribute zeros)
 #pragma unroll
       for (int d = 1; d < kMaxViewsPerPass; d <<= 1)
         m = pf::merge(m, pf::GroupMargin{__shfl_xor_sync(0xffffffffu, m.k, d), __shfl_xor_sync(0xffffffffu, m.g, d)});
       if (lane == 0) ws.gm = m;
+      if (MODE == kCacheRead) {
+        // Five planes when the scene bound clears the z-hi plane of every view of the group
+        // (read only where the cache is valid: cache_ok guards every use).
+        bool clear = false;
+        if (lane < nv && sc.box) {
+          float lo[3], hi[3];
+#pragma unroll
+          for (int k = 0; k < 3; ++k) {
+            hi[k] = pf::bound_value(__ldcg(sc.box_state + 1 + k));
+            lo[k] = pf::bound_value(~__ldcg(sc.box_state + 4 + k));
+          }
+          clear = pf::far_plane_clear(pl.q[2][1], lo, hi, pf::bound_value(__ldcg(sc.box_state + 7)), m);
+        }
+        const uint32_t all = nv >= 32 ? ~0u : (1u << nv) - 1u;
+        const uint32_t got = __ballot_sync(0xffffffffu, clear);
+        if (lane == 0) ws.far_off = (got & all) == all ? 1u : 0u;
+      }
     }
     __syncwarp();
     vkey = key;
   }
 
+  if (PF && MODE == kCacheFill) {  // the item's scene bound starts empty
+    if (lane < kBoundWords) ws.bnd[lane] = 0u;
+    __syncwarp();
+  }
   uint32_t qn = 0;
   uint4 xf = xf_first;
   for (uint32_t t = 0; t < n_t; ++t) {
@@ -612,6 +698,10 @@ __device__ __forceinline__ void warp_item(const CullLaunch& a, uint32_t item, Wa
   if (PF && qn) drain<MODE>(ws, sc, tile_first, qn, lane, cache_ok);
   else __syncwarp();
   finish_item<VPP>(ws, tile_first, n_t, nv, lane);
+  if (PF && MODE == kCacheFill && sc.box) {  // the item's bound into the scene's
+    __syncwarp();
+    if (lane < kBoundWords && ws.bnd[lane]) atomicMax(sc.box_state + 1 + lane, ws.bnd[lane]);
+  }
 }
 
 // The changed list of a view whose delta words fit one chunk, by one CTA (defined with the

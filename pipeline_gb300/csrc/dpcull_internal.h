@@ -87,6 +87,12 @@ constexpr uint32_t kErrWaitTimeout = 4u;    // a changed-list block gave up wait
 // host's choice of kernel.
 constexpr uint32_t kBoxStale = 0u;
 constexpr uint32_t kBoxValid = 1u;
+// The cache's state block: the state word, then the scene bound that the Fill launch
+// gathers with atomicMax (dpcull_prefilter.h bound_key): the largest centre x, y, z, the
+// complements of the smallest, the largest margin d0.  All zero when the cache goes stale.
+constexpr int kBoundWords = 7;
+constexpr size_t kCacheStateBytes = 32;
+static_assert((1 + kBoundWords) * 4 <= (int)kCacheStateBytes, "state word and bound fit the block");
 constexpr int kBoxRows = 5;
 constexpr int kObbFloats = 16;
 enum CacheMode : uint32_t { kCacheNone = 0u, kCacheFill = 1u, kCacheRead = 2u };
@@ -96,7 +102,7 @@ struct CullScene {
   const float* mats;       // [n_mats][16]
   float* box;              // prefilter-box cache [kBoxRows][cap], or nullptr (not cached)
   float* obb;              // OBB cache [cap][kObbFloats] (present with box)
-  uint32_t* box_state;     // the caches' state word (kBoxStale / kBoxValid)
+  uint32_t* box_state;     // the caches' state word (kBoxStale / kBoxValid) and scene bound
   uint32_t cap;            // SoA row stride (objects)
   uint32_t n_objects;
   uint32_t n_mats;

@@ -380,6 +380,73 @@ DPCULL_HD void decide_bits(float xl, float xh, float yl, float yh, float zl, flo
 #endif
 }
 
+// ---- leaving out the far plane --------------------------------------------------------
+// A group whose box cache is valid also keeps a bound of its scene (the box [lo, hi] of the
+// prefilter-box centres and the largest margin d0, over every box whose d0 is a number:
+// the pairs of the others are undecided whatever their plane values).  When the z-hi
+// plane value of every box in that bound is above its threshold D, that plane changes no
+// decision: max(zh, -zl) >= zh > D >= 0 >= -T, so with it o > D holds exactly when it
+// holds without it, and o <= -T likewise.  The cached kernel then evaluates five planes:
+// decide_bits5 gives the same bits as decide_bits for every box of the scene.
+//
+// far_plane_clear shows zh > D for every centre c in [lo, hi] and every d0 <= d0max
+// (D = fl(d0 K + G) grows with d0 as K >= 0).  The exact minimum of c.Q over the box is
+// Q_w + sum_k min(Q_k lo_k, Q_k hi_k); the kernel's FMA chain for zh and the sum below each
+// round by less than 4u M, M = |Q_w| + sum_k |Q_k| max(|lo_k|, |hi_k|), and the test keeps
+// 2^-16 M = 256u M in hand.  Any NaN (an empty bound, a view that cannot be bounded) makes
+// it false.
+DPCULL_HD bool far_plane_clear(const F4& q, const float (&lo)[3], const float (&hi)[3], float d0max,
+                               const GroupMargin& m)
+{
+  const float qa[3] = {q.x, q.y, q.z};
+  float lb = q.w, mag = std::fabs(q.w);
+  for (int k = 0; k < 3; ++k) {
+    const float a = qa[k] * lo[k], b = qa[k] * hi[k];
+    lb += a < b ? a : b;  // a NaN product makes lb NaN (no fmin: it would drop the NaN)
+    mag += std::fabs(qa[k]) * std::fmax(std::fabs(lo[k]), std::fabs(hi[k]));
+  }
+  return lb - mag * 0x1p-16f > std::fma(d0max, m.k, m.g);
+}
+
+// decide_bits without the z-hi plane, for boxes whose scene bound passed far_plane_clear.
+template <uint32_t BIT>
+DPCULL_HD void decide_bits5(float xl, float xh, float yl, float yh, float zl, float D, float negT,
+                            uint32_t& visible, uint32_t& undecided)
+{
+  const float o = std::fmin(std::fmin(std::fmin(xl, yl), zl), std::fmin(std::fmax(xh, -xl), std::fmax(yh, -yl)));
+#if defined(__CUDA_ARCH__)
+  asm("{\n\t.reg .pred pv, pu;\n\t"
+      "setp.gt.f32 pv, %2, %3;\n\t"
+      "setp.gtu.and.f32 pu, %2, %4, !pv;\n\t"
+      "@pv or.b32 %0, %0, %5;\n\t"
+      "@pu or.b32 %1, %1, %5;\n\t}"
+      : "+r"(visible), "+r"(undecided)
+      : "f"(o), "f"(D), "f"(negT), "n"(BIT));
+#else
+  const bool vis = o > D;
+  if (vis) visible |= BIT;
+  else if (!(o <= negT)) undecided |= BIT;
+#endif
+}
+
+// Order-preserving keys of the scene bound (the cache's bound words; all zero = empty):
+// key(f) grows with f, so atomicMax of key(c) keeps the largest centre and atomicMax of
+// ~key(c) the smallest.  NaN keys decode to NaN.
+DPCULL_HD uint32_t bound_key(float f)
+{
+  uint32_t b;
+  memcpy(&b, &f, sizeof b);
+  return (b & 0x80000000u) ? ~b : b | 0x80000000u;
+}
+
+DPCULL_HD float bound_value(uint32_t key)
+{
+  const uint32_t b = (key & 0x80000000u) ? key & 0x7FFFFFFFu : ~key;
+  float f;
+  memcpy(&f, &b, sizeof f);
+  return f;
+}
+
 // Whole classification of one box in one view of a group with margin m.
 DPCULL_HD int classify_group(const Box& b, const Planes& p, const GroupMargin& m)
 {

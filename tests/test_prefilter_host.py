@@ -254,3 +254,89 @@ def test_group_margin_is_the_largest(pf):
         alone = classify(pf, *scene, vp)
         dec = cls[k] != 2
         assert np.array_equal(cls[k][dec], alone[dec])
+
+
+# ---- leaving out the far plane (pf::far_plane_clear) ---------------------------------------
+
+def _far(lib):
+    lib.pf_far_scene.argtypes = [ctypes.c_size_t] + [ctypes.c_void_p] * 5 + [ctypes.c_size_t, ctypes.c_void_p,
+                                                                            ctypes.c_void_p]
+    lib.pf_far_scene.restype = None
+    lib.pf_far_fuzz.argtypes = [ctypes.c_uint64, ctypes.c_int64, ctypes.c_void_p]
+    lib.pf_far_fuzz.restype = ctypes.c_int64
+    return lib
+
+
+def far_scene(lib, scene, vps):
+    """Per view: whether the scene bound clears its z-hi plane, and the boxes for which
+    that would change a decision (must be 0)."""
+    lower, extent, xform, mats = [np.ascontiguousarray(a) for a in scene]
+    vps = np.ascontiguousarray(np.asarray(vps, np.float32).reshape(-1, 16))
+    clear = np.zeros(vps.shape[0], np.int32)
+    bad = np.zeros(vps.shape[0], np.int64)
+    _far(lib).pf_far_scene(lower.shape[1], lower.ctypes.data, extent.ctypes.data, xform.ctypes.data,
+                           mats.ctypes.data, vps.ctypes.data, vps.shape[0], clear.ctypes.data, bad.ctypes.data)
+    return clear.astype(bool), bad
+
+
+def test_far_plane_left_out_for_the_stress_views(pf):
+    """The stress scene (a 2^20-object chunk of it, all its shared matrices) under its cube
+    faces and stereo pair, jittered: the scene lies far inside every far plane, so every
+    view is cleared and the cached kernel tests five planes; every box's five-plane bits
+    equal its six-plane bits."""
+    sc = wl.stress_scene(n_objects=1 << 20, n_transforms=1 << 16)
+    scene = (sc["lower"], sc["extent"], sc["xform"], sc["mats"])
+    rng = np.random.default_rng(21)
+    for vps in (sc["vps"], [wl.jitter_view(rng, v) for v in sc["vps"]]):
+        clear, bad = far_scene(pf, scene, vps)
+        assert clear.all(), clear
+        assert not bad.any(), bad
+
+
+def test_far_plane_kept_where_it_cuts_the_scene(pf):
+    """Views whose far plane passes through the scene keep it, those whose far plane lies
+    past every centre leave it out, and no decision differs either way (cascades too)."""
+    rng = np.random.default_rng(22)
+    n = 50_000
+    lower, _, extent = wl.random_boxes(rng, n)
+    mats = wl.random_matrices(rng, 4096)
+    xform = rng.integers(0, 4096, n).astype(np.uint32)
+    scene = (lower, extent, xform, mats)
+    # the centres fill [-1005, 1005]^3 and the camera looks down -z from the origin
+    near_far = [wl.perspective(60.0, 16 / 9, 0.1, far) for far in (300.0, 900.0, 1004.0)]
+    clear, bad = far_scene(pf, scene, near_far)
+    assert not clear.any() and not bad.any()
+    clear, bad = far_scene(pf, scene, wl.cascade_views())
+    assert not bad.any()
+    # far planes past the scene's last centre are cleared
+    clear, bad = far_scene(pf, scene, [wl.perspective(60.0, 16 / 9, 0.1, far) for far in (1100.0, 5000.0)])
+    assert clear.all() and not bad.any()
+
+
+def test_far_plane_clear_fuzz(pf):
+    """Random bounds, plane normals (unit and shorter), offsets around the bound and
+    margins: wherever the test clears a plane, the bound's corners and random centres in it
+    have plane values above D for every margin up to d0max."""
+    viol = np.zeros(1, np.int64)
+    cleared = _far(pf).pf_far_fuzz(7, 400_000, viol.ctypes.data)
+    assert viol[0] == 0
+    assert cleared > 50_000, cleared
+
+
+def test_bound_keys_order_and_round_trip():
+    """The bound keys of the Fill launch's atomicMax (the formula of pf::bound_key) keep the
+    order of the floats; decoding is covered by the scene tests above."""
+    import struct
+    rng = np.random.default_rng(23)
+    vals = np.concatenate([rng.normal(0, 1e3, 2000), rng.normal(0, 1e-30, 200), [-0.0, 0.0, 3e38, -3e38, 1e-45]])
+    vals = vals.astype(np.float32)  # -0.0 before 0.0: their keys order them that way
+
+    def key(f):
+        b = struct.unpack("<I", struct.pack("<f", float(f)))[0]
+        return (~b & 0xFFFFFFFF) if b & 0x80000000 else b | 0x80000000
+
+    keys = np.array([key(v) for v in vals], np.uint64)
+    order = np.argsort(vals, kind="stable")
+    ks = keys[order]
+    assert np.all(ks[1:] >= ks[:-1])
+    assert key(-0.0) < key(0.0) < key(1e-45)
