@@ -768,12 +768,22 @@ __global__ void __launch_bounds__(kThreads, MODE == kCacheRead ? 4 : 3) cull_ker
 }
 
 // ---- changed-list assembly ----------------------------------------------------------------
-// The delta words are grouped in chunks of kDeltaChunk (one block, 16 words per thread).
-// One pass: the blocks of a view take its chunks in the order they start (a ticket), count
-// their chunk's changed objects and publish the count, then add the earlier chunks' counts
+// One pass over a view's delta words in chunks of kEmitChunk words, one block each: the
+// blocks of a view take their chunks in the order they start (a ticket), count their
+// chunk's changed objects and publish the count, then add the earlier chunks' counts
 // (published by blocks that started before them, so the wait always ends) and write every
 // changed index, ascending.  The view's last block clears the counts for the next launch.
+// Each warp owns 1024 consecutive words of its block's chunk, read in 8 rounds of one
+// coalesced uint4 per lane, and writes each round's changed indices after a warp scan, so
+// the lanes of a warp store into one stretch of the list.  Blocks of 256 threads with at
+// most 64 registers: 4 per SM, so the 16M-object stress views (62 chunks x 8 views) run in
+// one wave.  The small-launch path in the cull's last CTA (emit_small_view) keeps chunks
+// of kDeltaChunk words, 16 per thread.
 constexpr int kScanThreads = 256;
+constexpr int kEmitRounds = 8;                                        // uint4 rounds per warp
+constexpr uint32_t kEmitWarpWords = 32u * 4u * kEmitRounds;           // 1024
+constexpr uint32_t kEmitChunk = kScanThreads / 32 * kEmitWarpWords;   // 8192 words per block
+static_assert(kEmitChunk % kDeltaChunk == 0, "a view's emit chunks fit its scratch counts");
 constexpr int kWordsPerThread = kDeltaChunk / kScanThreads;
 static_assert(kWordsPerThread % 4 == 0, "whole uint4 loads");
 constexpr uint32_t kSpinLimit = 1u << 20;  // polls of an earlier chunk's count (~0.1 s)
@@ -809,11 +819,36 @@ __device__ __forceinline__ uint32_t block_scan(uint32_t x, uint32_t* wsum, uint3
   return wsum[warp] + incl - x;
 }
 
-// grid = (chunks, views)
-__global__ void __launch_bounds__(kScanThreads)
+// A warp's 8 rounds of delta words from word `base` (n_words is a multiple of 4 and the
+// array 16-byte aligned, so a round's uint4 is whole or past the end).
+__device__ __forceinline__ void load_rounds(const uint32_t* delta, uint32_t n_words, uint32_t base, int lane,
+                                            uint4 (&q)[kEmitRounds])
+{
+#pragma unroll
+  for (int k = 0; k < kEmitRounds; ++k) {
+    const uint32_t i = base + (uint32_t)k * 128u + 4u * (uint32_t)lane;
+    q[k] = i < n_words ? __ldcg(reinterpret_cast<const uint4*>(delta + i)) : make_uint4(0u, 0u, 0u, 0u);
+  }
+}
+
+// The set bits of one delta word as object indices at out[p], out[p + 1], ...
+__device__ __forceinline__ void emit_word(uint32_t m, uint32_t word, uint32_t* changed, uint32_t* copy, uint32_t& p)
+{
+  while (m) {
+    const uint32_t obj = word * 32u + (uint32_t)(__ffs(m) - 1);
+    changed[p] = obj;
+    if (copy) copy[p] = obj;
+    ++p;
+    m &= m - 1u;
+  }
+}
+
+// grid = (chunks of kEmitChunk words, views)
+__global__ void __launch_bounds__(kScanThreads, 4)
     emit_changed_kernel(const CullView* views, const __grid_constant__ CullView one, unsigned int* err)
 {
-  __shared__ uint32_t wsum[kScanThreads / 32];
+  __shared__ uint32_t woff[kScanThreads / 32];
+  __shared__ uint32_t wbefore[kScanThreads / 32];
   __shared__ uint32_t tot;
   __shared__ uint32_t chunk;
   __shared__ bool last;
@@ -821,7 +856,8 @@ __global__ void __launch_bounds__(kScanThreads)
   asm volatile("griddepcontrol.wait;" ::: "memory");
   const CullView& v = views ? views[blockIdx.y] : one;
   if (v.flags & kViewNoChanged) return;  // uniform
-  const uint32_t n_chunks = (uint32_t)chunks_of(v.n_words);
+  const uint32_t n_words = v.n_words;
+  const uint32_t n_chunks = (n_words + kEmitChunk - 1) / kEmitChunk;
   if (blockIdx.x >= n_chunks) {  // uniform; only the view's first n_chunks blocks take tickets
     if (blockIdx.x == 0 && threadIdx.x == 0) {
       *v.n_changed = 0;
@@ -829,19 +865,36 @@ __global__ void __launch_bounds__(kScanThreads)
     }
     return;
   }
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   uint32_t* state = v.chunk_tot;  // per chunk: its count + 1 once published
   uint32_t* ticket = state + n_chunks;
   uint32_t* done = ticket + 1;
+  const uint32_t* delta = v.delta;
   if (threadIdx.x == 0) chunk = atomicAdd(ticket, 1u);
+  // Blocks nearly always start in index order, so the ticket gives this block's own chunk:
+  // its words load while the ticket is taken (and again in the rare other case).
+  uint4 q[kEmitRounds];
+  load_rounds(delta, n_words, blockIdx.x * kEmitChunk + (uint32_t)warp * kEmitWarpWords, lane, q);
   __syncthreads();
   const uint32_t c = chunk;
-  const uint32_t b = c * kDeltaChunk + threadIdx.x * kWordsPerThread;
-  uint32_t w[kWordsPerThread];
-  load_delta(v, b, w);
-  uint32_t s = 0;
+  if (c != blockIdx.x) load_rounds(delta, n_words, c * kEmitChunk + (uint32_t)warp * kEmitWarpWords, lane, q);
+  uint32_t cnt[kEmitRounds];
+  uint32_t mine = 0;
 #pragma unroll
-  for (int j = 0; j < kWordsPerThread; ++j) s += (uint32_t)__popc(w[j]);
-  const uint32_t in_block = block_scan(s, wsum, &tot);
+  for (int k = 0; k < kEmitRounds; ++k) {
+    cnt[k] = (uint32_t)(__popc(q[k].x) + __popc(q[k].y) + __popc(q[k].z) + __popc(q[k].w));
+    mine += cnt[k];
+  }
+  const uint32_t wtot = __reduce_add_sync(0xffffffffu, mine);
+  if (lane == 0) woff[warp] = wtot;
+  __syncthreads();
+  if (warp == 0) {
+    const uint32_t x = lane < kScanThreads / 32 ? woff[lane] : 0u;
+    const uint32_t incl = warp_scan(x, lane);
+    if (lane < kScanThreads / 32) woff[lane] = incl - x;
+    if (lane == 31) tot = incl;
+  }
+  __syncthreads();
   const uint32_t count = tot;
   if (threadIdx.x == 0) atomicExch(state + c, count + 1u);
   // Changed objects of the earlier chunks: their blocks took earlier tickets, so they are
@@ -862,35 +915,44 @@ __global__ void __launch_bounds__(kScanThreads)
     before += x - 1u;
   }
   if (gave_up) atomicOr(err, kErrWaitTimeout);
-  __syncthreads();  // every thread has read tot
-  block_scan(before, wsum, &tot);
-  const uint32_t base = tot;
+  const uint32_t wb = __reduce_add_sync(0xffffffffu, before);
+  if (lane == 0) wbefore[warp] = wb;
+  __syncthreads();
+  uint32_t base = 0;
+#pragma unroll
+  for (int i = 0; i < kScanThreads / 32; ++i) base += wbefore[i];
   if (threadIdx.x == 0 && c == n_chunks - 1) {
     const uint32_t n = base + count;
     *v.n_changed = n;
     if (v.copy_count) *v.copy_count = n;
   }
+  // This block has read every count it needs; the count of finished blocks tells the last
+  // one (its return value is waited for only after the writes).
+  uint32_t finished = 0;
+  if (threadIdx.x == 0) finished = atomicAdd(done, 1u);
+  uint32_t* const changed = v.changed;
+  uint32_t* const copy = v.copy_changed;
+  uint32_t pos = base + woff[warp];
+  const uint32_t wbase = c * kEmitChunk + (uint32_t)warp * kEmitWarpWords + 4u * (uint32_t)lane;
+#pragma unroll
+  for (int k = 0; k < kEmitRounds; ++k) {
+    const uint32_t incl = warp_scan(cnt[k], lane);
+    uint32_t p = pos + incl - cnt[k];
+    pos += __shfl_sync(0xffffffffu, incl, 31);
+    const uint32_t wd = wbase + (uint32_t)k * 128u;
+    emit_word(q[k].x, wd, changed, copy, p);
+    emit_word(q[k].y, wd + 1u, changed, copy, p);
+    emit_word(q[k].z, wd + 2u, changed, copy, p);
+    emit_word(q[k].w, wd + 3u, changed, copy, p);
+  }
   // The last block past its reads clears the counts, the ticket and the block count.
-  if (threadIdx.x == 0) last = atomicAdd(done, 1u) == n_chunks - 1;
+  if (threadIdx.x == 0) last = finished == n_chunks - 1;
   __syncthreads();
   if (last) {
     for (uint32_t i = threadIdx.x; i < n_chunks; i += kScanThreads) state[i] = 0u;
     if (threadIdx.x == 0) {
       *ticket = 0u;
       *done = 0u;
-    }
-  }
-  uint32_t pos = base + in_block;
-#pragma unroll
-  for (int j = 0; j < kWordsPerThread; ++j) {
-    uint32_t m = w[j];
-    while (m) {
-      const int k = __ffs(m) - 1;
-      const uint32_t obj = (b + (uint32_t)j) * 32u + (uint32_t)k;
-      v.changed[pos] = obj;
-      if (v.copy_changed) v.copy_changed[pos] = obj;
-      ++pos;
-      m &= m - 1u;
     }
   }
 }
@@ -1035,7 +1097,7 @@ int launch_changed_lists(const CullView* views, const CullView& one, uint32_t n_
 {
   cudaStream_t s = static_cast<cudaStream_t>(stream);
   if (!n_views) return 0;
-  const uint32_t chunks = std::max<uint32_t>(1, (uint32_t)chunks_of(max_words));
+  const uint32_t chunks = std::max<uint32_t>(1, (max_words + kEmitChunk - 1) / kEmitChunk);
   cudaLaunchConfig_t cfg = {};
   cfg.gridDim = dim3(chunks, n_views);
   cfg.blockDim = dim3(kScanThreads);
