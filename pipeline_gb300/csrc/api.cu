@@ -1327,9 +1327,10 @@ static int plan_capture(dpcull_ctx c, Plan& p, int slot, CacheMode mode)
   CU(cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking));
   cudaGraph_t graph = nullptr;
   cudaError_t e = cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal);
-  if (e == cudaSuccess)
-    e = cudaMemcpyAsync(p.d_views, p.h_views[slot], p.views.size() * sizeof(CullView),
-                        cudaMemcpyHostToDevice, cs);
+  if (e == cudaSuccess &&
+      launch_copy_words(reinterpret_cast<uint32_t*>(p.d_views), reinterpret_cast<const uint32_t*>(p.h_views[slot]),
+                        p.views.size() * sizeof(CullView) / 4, cs))
+    e = cudaGetLastError() == cudaSuccess ? cudaErrorLaunchFailure : cudaGetLastError();
   int rc = DPCULL_OK;
   if (e == cudaSuccess) {
     const uint64_t before = c->launches;
@@ -1573,8 +1574,9 @@ int dpcull_plan_launch(dpcull_ctx c, dpcull_plan ph)
   note_launch(c, p->groups, p->scenes, mode);
   p->pending[s] = true;
   p->next ^= 1;
-  // the graph's kernels: the cull, and the changed lists unless the cull builds them
-  c->launches += fused_emit_views((uint32_t)p->views.size(), max_words_of(p->scenes)) ? 1 : 2;
+  // the graph's kernels: the view copy, the cull, and the changed lists unless the cull
+  // builds them
+  c->launches += fused_emit_views((uint32_t)p->views.size(), max_words_of(p->scenes)) ? 2 : 3;
   return DPCULL_OK;
 }
 

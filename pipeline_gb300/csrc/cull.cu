@@ -1057,6 +1057,14 @@ __global__ void snapshot_kernel(const ResultCopy* copies)
     c.dst_changed[i] = __ldcg(c.changed + i);
 }
 
+// A plan's views from their pinned host slot into device memory (the first node of the
+// plan's graph): a kernel reads the host buffer directly, which starts the cull sooner
+// than a copy-engine transfer of the same ~1 KB would.
+__global__ void copy_words_kernel(uint32_t* dst, const uint32_t* src, uint32_t n)
+{
+  for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) dst[i] = src[i];
+}
+
 // GroupBitSet::removeObject moves the last object into the hole: SoA row copy.
 __global__ void move_object_kernel(float* soa, uint32_t cap, uint32_t from, uint32_t to)
 {
@@ -1108,6 +1116,14 @@ int launch_changed_lists(const CullView* views, const CullView& one, uint32_t n_
   cfg.attrs = attr;
   cfg.numAttrs = 1;
   if (cudaLaunchKernelEx(&cfg, emit_changed_kernel, views, one, err) != cudaSuccess) return -1;
+  return cudaGetLastError() == cudaSuccess ? 0 : -1;
+}
+
+int launch_copy_words(uint32_t* dst, const uint32_t* src, size_t n_words, void* stream)
+{
+  if (!n_words) return 0;
+  const unsigned blocks = (unsigned)std::min<size_t>(64, (n_words + 4095) / 4096);
+  copy_words_kernel<<<blocks, 256, 0, static_cast<cudaStream_t>(stream)>>>(dst, src, (uint32_t)n_words);
   return cudaGetLastError() == cudaSuccess ? 0 : -1;
 }
 

@@ -238,6 +238,10 @@ size_t bbox_partials_needed(uint32_t n_objects);
 int launch_bbox(const float* soa, uint32_t cap, uint32_t n, const float* mats, float* partials,
                 unsigned int* counter, float* out8, void* stream);
 
+// n_words 32-bit words from src (device memory, or page-locked host memory, which the
+// kernel reads directly) to dst (device memory).
+int launch_copy_words(uint32_t* dst, const uint32_t* src, size_t n_words, void* stream);
+
 // Result remap on object removal (api helpers in cull.cu).
 int launch_move_bit(uint32_t* bits, uint32_t size_bits, uint32_t old_index, uint32_t new_index,
                     void* stream);
