@@ -505,6 +505,9 @@ __device__ __forceinline__ uint32_t classify_tile(const CullLaunch& a, WarpShare
       const pf::F4 m2{r2.x, r2.y, r2.z, r2.w}, m3{r3.x, r3.y, r3.z, r3.w};
       bx[k] = pf::make_box(comp(lx, k), comp(ly, k), comp(lz, k), comp(ex, k), comp(ey, k),
                            comp(ez, k), m0, m1, m2, m3);
+      // Boxes stored in the cache are read by every later launch: the tighter radius pays.
+      if (MODE == kCacheFill && sc.box)
+        bx[k].r = pf::tight_radius(comp(ex, k), comp(ey, k), comp(ez, k), m0, m1, m2, bx[k].r);
       if (MODE == kCacheFill && use && sc.box)
         store_obb(sc, obj0 + k, make_obb(comp(lx, k), comp(ly, k), comp(lz, k), comp(ex, k), comp(ey, k),
                                          comp(ez, k), r0, r1, r2, r3));

@@ -215,6 +215,31 @@ DPCULL_HD Box make_box(float lx, float ly, float lz, float ex, float ey, float e
   return b;
 }
 
+// A tighter radius for boxes that are built once and kept (the group's box cache): every
+// corner offset from the centre is (s1 X + s2 Y + s3 Z) / 2, so R may be half the largest
+// of the four norms ||s1 X + s2 Y + Z|| (the 8 sign patterns in +- pairs) instead of
+// (||X|| + ||Y|| + ||Z||) / 2 -- up to sqrt(3) smaller for the rotations and scales of a
+// scene graph.  Each component of s1 X + s2 Y + Z is computed from the reference's rounded
+// X_j = fl(ex M_0j) (exact up to the sign) and two FMAs with the exact products e M, so it
+// is within 3u (|X_j| + |Y_j| + |Z_j|) of the real value, and the error vector's norm is
+// at most 3u (||X|| + ||Y|| + ||Z||) <= 6u R_loose; the added 2^-20 r_loose covers it.
+// Each norm is bounded like row_norm (sqrt_bound, then 2^-18), and the result is inflated
+// by (1 + 2^-18) twice like the loose radius.  Never above r_loose (a NaN gives r_loose).
+DPCULL_HD float tight_radius(float ex, float ey, float ez, const F4& m0, const F4& m1, const F4& m2, float r_loose)
+{
+  const float X[3] = {ex * m0.x, ex * m0.y, ex * m0.z};
+  float nmax = 0.f;
+  for (int s = 0; s < 4; ++s) {
+    const float sx = (s & 1) ? -1.f : 1.f, sy = (s & 2) ? -ey : ey;
+    const float vx = std::fma(ez, m2.x, std::fma(sy, m1.x, sx * X[0]));
+    const float vy = std::fma(ez, m2.y, std::fma(sy, m1.y, sx * X[1]));
+    const float vz = std::fma(ez, m2.z, std::fma(sy, m1.z, sx * X[2]));
+    nmax = std::fmax(nmax, sqrt_bound(std::fma(vx, vx, std::fma(vy, vy, std::fma(vz, vz, 0x1p-120f)))) * kInflate);
+  }
+  const float r = (0.5f * nmax + r_loose * 0x1p-20f) * kInflate * kInflate;
+  return std::fmin(r, r_loose);
+}
+
 // Plane value L = c.Q (c.w == 1: Q_w is the addend).
 DPCULL_HD float plane(const Box& b, const F4& q)
 {

@@ -9,6 +9,19 @@
 
 using dpcull::pf::F4;
 
+// The prefilter box of one object as the kernels build it: built with
+// -DPF_TIGHT, the radius the Fill launch stores in the box cache (pf::tight_radius),
+// otherwise the one the fused kernel uses every launch.
+static dpcull::pf::Box box_of(float lx, float ly, float lz, float ex, float ey, float ez, const F4& m0,
+                              const F4& m1, const F4& m2, const F4& m3)
+{
+  dpcull::pf::Box b = dpcull::pf::make_box(lx, ly, lz, ex, ey, ez, m0, m1, m2, m3);
+#ifdef PF_TIGHT
+  b.r = dpcull::pf::tight_radius(ex, ey, ez, m0, m1, m2, b.r);
+#endif
+  return b;
+}
+
 // Classification of n objects (planar [3][n] lower / extent rows, transform indices into
 // mats[][16]) in one view: 0 invisible, 1 visible, 2 undecided.
 extern "C" void pf_classify_soa(size_t n, const float* lower, const float* extent,
@@ -21,7 +34,7 @@ extern "C" void pf_classify_soa(size_t n, const float* lower, const float* exten
     const float* m = mats + 16 * (size_t)idx[i];
     const F4 m0{m[0], m[1], m[2], m[3]}, m1{m[4], m[5], m[6], m[7]};
     const F4 m2{m[8], m[9], m[10], m[11]}, m3{m[12], m[13], m[14], m[15]};
-    const dpcull::pf::Box b = dpcull::pf::make_box(lower[i], lower[n + i], lower[2 * n + i],
+    const dpcull::pf::Box b = box_of(lower[i], lower[n + i], lower[2 * n + i],
                                                    extent[i], extent[n + i], extent[2 * n + i],
                                                    m0, m1, m2, m3);
     out[i] = (int8_t)dpcull::pf::classify(b, p);
@@ -45,7 +58,7 @@ extern "C" void pf_classify_group_soa(size_t n, const float* lower, const float*
     const float* m = mats + 16 * (size_t)idx[i];
     const F4 m0{m[0], m[1], m[2], m[3]}, m1{m[4], m[5], m[6], m[7]};
     const F4 m2{m[8], m[9], m[10], m[11]}, m3{m[12], m[13], m[14], m[15]};
-    const dpcull::pf::Box b = dpcull::pf::make_box(lower[i], lower[n + i], lower[2 * n + i],
+    const dpcull::pf::Box b = box_of(lower[i], lower[n + i], lower[2 * n + i],
                                                    extent[i], extent[n + i], extent[2 * n + i],
                                                    m0, m1, m2, m3);
     for (size_t v = 0; v < n_views && v < 64; ++v)
@@ -69,7 +82,7 @@ extern "C" void pf_far_scene(size_t n, const float* lower, const float* extent, 
     const float* m = mats + 16 * (size_t)idx[i];
     const F4 m0{m[0], m[1], m[2], m[3]}, m1{m[4], m[5], m[6], m[7]};
     const F4 m2{m[8], m[9], m[10], m[11]}, m3{m[12], m[13], m[14], m[15]};
-    const Box b = make_box(lower[i], lower[n + i], lower[2 * n + i], extent[i], extent[n + i],
+    const Box b = box_of(lower[i], lower[n + i], lower[2 * n + i], extent[i], extent[n + i],
                            extent[2 * n + i], m0, m1, m2, m3);
     boxes[i] = b;
     if (b.d0 == b.d0) {
