@@ -63,6 +63,7 @@ struct WarpShared {
   pf::GroupMargin gm;                                    // margin of the staged view group
   uint32_t words[kMaxViewsPerPass][kItemTiles][kTileWords];  // the item's visibility words
   uint16_t queue[kQueueCap];                             // tile << 10 | object << 3 | view
+  uint32_t qtail;                                        // the queue's length (slots taken)
   ulonglong2 qp[kMaxViewsPerPass][3][2];                 // per axis: (lo, hi) pairs of x, y | z, w
   float4 zlo[kMaxViewsPerPass];                          // the z-lo planes alone (five-plane test)
   uint32_t far_off;                                      // the group may leave out its z-hi planes
@@ -348,20 +349,23 @@ __device__ __forceinline__ void drain(WarpShared& ws, const CullScene& sc, uint3
 }
 
 // The lane's undecided pairs of tile t into the warp's queue (drained early only if it
-// would overflow).  Returns the new queue length.
+// would overflow).  Each lane with pairs takes its slots with one shared-memory atomicAdd
+// on the queue's length, so the pairs of a tile land in lane order only by chance; the
+// order does not matter (each pair sets its own bit).  Returns the new queue length.
 template <int VPP, uint32_t MODE>
 __device__ __forceinline__ uint32_t push_undecided(WarpShared& ws, const CullScene& sc, uint32_t tile_first,
                                                    uint32_t t, uint32_t qn, uint32_t amb, int lane, bool obbs)
 {
   const uint32_t cnt = (uint32_t)__popc(amb);
-  const uint32_t incl = warp_scan(cnt, lane);
-  const uint32_t tot = __shfl_sync(0xffffffffu, incl, 31);
+  const uint32_t tot = __reduce_add_sync(0xffffffffu, cnt);
   if (tot) {  // uniform over the warp
     if (qn + tot > (uint32_t)kQueueCap) {
       drain<MODE>(ws, sc, tile_first, qn, lane, obbs);
       qn = 0;
+      if (lane == 0) ws.qtail = 0u;
+      __syncwarp();
     }
-    uint32_t pos = qn + incl - cnt;
+    uint32_t pos = cnt ? atomicAdd(&ws.qtail, cnt) : 0u;
     while (amb) {
       const int b = __ffs(amb) - 1;
       ws.queue[pos++] = (uint16_t)((t << 10) | (((uint32_t)lane * kObjPerThread + und_object<VPP>(b)) << 3) |
@@ -691,6 +695,8 @@ __device__ __forceinline__ void warp_item(const CullLaunch& a, uint32_t item, Wa
     __syncwarp();
   }
   uint32_t qn = 0;
+  if (lane == 0) ws.qtail = 0u;
+  __syncwarp();
   uint4 xf = xf_first;
   for (uint32_t t = 0; t < n_t; ++t) {
     uint4 xf_next = make_uint4(0u, 0u, 0u, 0u);
