@@ -28,7 +28,10 @@ def test_pipe_bounds_from_the_committed_capture(kernel):
     # one warp-instruction per scheduler per cycle: the capture's own issue fraction
     assert abs(issue["frac"] - d["warp_instructions_per_launch"] / (d["sm_cycles_elapsed"] * 4 * 152)) < 1e-9
     assert 30 < issue["thread_instructions_per_object_view"] < 120
-    assert 0 < fp32["frac"] < 1 and fp32["ops_per_object_view"] > 18  # 18 FMAs of the planes at least
+    # the plane FMAs at least: six planes (18) in the fused kernel, five (15) in the cached one,
+    # which leaves out the far plane of the stress views (their scene bound clears it)
+    planes = 15 if kernel == "warm" else 18
+    assert 0 < fp32["frac"] < 1 and fp32["ops_per_object_view"] > planes
     # scaled to the 16M-object workload: same per-object-view figures
     issue16, fp16 = bench.pipe_bounds(_Workload(16_000_000, 8), 1.0, 2070.0, 152, kernel)
     assert abs(issue16["thread_instructions_per_object_view"] - issue["thread_instructions_per_object_view"]) < 0.01
