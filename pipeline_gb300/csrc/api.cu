@@ -682,9 +682,10 @@ std::string tune_key(const std::vector<CullScene>& scenes, const std::vector<Cul
   }
   const int bucket = objs ? (int)std::floor(std::log2((double)objs)) : 0;
   char buf[112];
-  // "w512": tunings of the kernel whose warp items are 512 objects; "bc": of the kernel
+  // "w1024": tunings of the kernel whose warp items are up to 1024 objects; "bc": of the kernel
   // that reads the box caches (the steady state of a plan whose scenes all keep one)
-  snprintf(buf, sizeof buf, "w512_n2^%d_v%zu_maxv%u_s%zu%s", bucket, views.size(), maxv, scenes.size(),
+  snprintf(buf, sizeof buf, "w%d_n2^%d_v%zu_maxv%u_s%zu%s", kItemTiles * kTileObjects, bucket, views.size(), maxv,
+           scenes.size(),
            cached ? "_bc" : "");
   return buf;
 }

@@ -2,7 +2,7 @@
 //
 // One kernel serves the plain per-call path (one group, one view) and the batched
 // persistent path (many groups x many views).  Every warp works on its own: it pulls work
-// items from an atomic ticket, and a work item is 1-4 tiles of 128 objects (one float4 of
+// items from an atomic ticket, and a work item is 1-8 tiles of 128 objects (one float4 of
 // each SoA row per lane; the launch picks the tiles per item) of one scene with one group
 // of up to VPP views:
 //   1. stage the views (view-projection matrices, output pointers) and their prefilter
@@ -558,8 +558,9 @@ __device__ __forceinline__ uint32_t classify_tile(const CullLaunch& a, WarpShare
 
 // The final words of the item, per view: the new words (stored only where they changed),
 // the delta words (old XOR new, every word) and, for serving launches, the visible count.
-// The lanes take (view, word) pairs: a view's words occupy 16 lanes (4 for a single-tile
-// item), so 2 (8) views go per pass and the 8 views of an item take 4 passes (1).  Every
+// The lanes take (view, word) pairs: a view's words occupy 32 lanes (16 for an item of 2
+// to 4 tiles, 4 for a single-tile item), so 1 (2, 8) views go per pass and the 8 views of
+// an item take 8 passes (4, 1).  Every
 // pass's previous words are loaded before any store, so the loads are in flight together.
 template <int VPP>
 __device__ __forceinline__ void finish_item(const WarpShared& ws, uint32_t tile_first, uint32_t n_t,
@@ -567,7 +568,7 @@ __device__ __forceinline__ void finish_item(const WarpShared& ws, uint32_t tile_
 {
   constexpr int kPasses = (VPP * kItemTiles * kTileWords + 31) / 32;
   const uint32_t wpv = n_t * kTileWords;  // the item's words per view
-  const int sh = n_t == 1 ? 2 : 4;        // lanes per view: 4 or 16
+  const int sh = n_t == 1 ? 2 : n_t <= 4 ? 4 : 5;  // lanes per view: 4, 16 or 32
   const uint32_t base = tile_first * kTileWords;
   uint32_t prev[kPasses];
 #pragma unroll

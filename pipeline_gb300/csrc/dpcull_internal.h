@@ -32,7 +32,7 @@ constexpr int kWarpsPerCta = kThreads / 32;
 constexpr int kObjPerThread = 4;                   // one float4 of each SoA row
 constexpr int kTileObjects = 32 * kObjPerThread;   // 128 objects per tile (one warp)
 constexpr int kTileWords = kTileObjects / 32;      // 4 bit-array words per tile and view
-constexpr int kItemTiles = 4;                      // tiles per work item (one warp, one view group)
+constexpr int kItemTiles = 8;                      // tiles per work item (one warp, one view group)
 constexpr int kQueueCap = 1024;                    // undecided pairs a warp holds before a drain
 constexpr uint32_t kDeltaChunk = 4096;             // delta words per changed-list chunk
 
@@ -58,7 +58,8 @@ DPCULL_HD_CONST uint32_t tile_groups_of(uint32_t n_tiles, uint32_t n_big, uint32
 inline uint32_t item_tiles_for(uint64_t tile_groups, int sm_count)
 {
   const uint64_t warps = (uint64_t)(sm_count > 0 ? sm_count : 1) * 24;
-  if (tile_groups >= warps * 8) return kItemTiles;
+  if (tile_groups >= warps * 16) return kItemTiles;
+  if (tile_groups >= warps * 8) return 4;
   if (tile_groups >= warps * 4) return 2;
   return 1;
 }

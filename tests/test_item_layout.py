@@ -99,14 +99,14 @@ def test_layout_random_scene_lists(lib):
 
 
 def test_layout_stress_workload(lib):
-    """16M objects, one view group, 152 SMs: 4-tile items and a 9728-unit single-tile tail."""
+    """16M objects, one view group, 152 SMs: 8-tile items and a 9728-unit single-tile tail."""
     tiles = 16_000_000 // 128
     it = lib.tiles_for(tiles, 152)
     tail = lib.tail_for(152)
-    assert it == 4 and tail == 152 * 64
+    assert it == 8 and tail == 152 * 64
     n_big, items = check(lib, [tiles], [1], it, tail)
-    assert n_big[0] == (tiles - tail) // 4
-    assert items == n_big[0] + (tiles - n_big[0] * 4)
+    assert n_big[0] == (tiles - tail) // 8
+    assert items == n_big[0] + (tiles - n_big[0] * 8)
 
 
 def test_layout_without_tail_keeps_full_items(lib):
