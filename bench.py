@@ -221,7 +221,9 @@ def run_ours(args, dist: Dist) -> dict | None:
         ctx.plan_set_views(wl.plan, frames[i])
         ctx.plan_launch(wl.plan)
     ctx.synchronize()
-    ev = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps + 1)]
+    # Two events bracket the timed steps: an event recorded between graph launches costs
+    # ~2 us of device time per step, so the per-step latencies come from a separate loop.
+    ev = [torch.cuda.Event(enable_timing=True) for _ in range(2)]
     clocks = Clocks(device)
     clocks.start()
     dist.barrier()
@@ -234,18 +236,29 @@ def run_ours(args, dist: Dist) -> dict | None:
         for i in range(args.steps):
             ctx.plan_set_views(wl.plan, frames[args.warmup + i])
             ctx.plan_launch(wl.plan)
-            ev[i + 1].record(stream)
             if i:  # the cull kernel of the previous step (events inside the plan's graph)
                 kernel_ms.append(ctx.plan_kernel_ms(wl.plan, 1))
+        ev[1].record(stream)
     ctx.synchronize()
     torch.cuda.synchronize()
     kernel_ms.append(ctx.plan_kernel_ms(wl.plan, 0))
     launches = ctx.kernel_launches - launches0
     kinds = {k: v - kinds0[k] for k, v in ctx.cull_launches().items()}
     clk = clocks.stop()
-    step_ms = [ev[i].elapsed_time(ev[i + 1]) for i in range(args.steps)]
-    total_ms = ev[0].elapsed_time(ev[args.steps])
+    total_ms = ev[0].elapsed_time(ev[1])
     total_ms = dist.max(total_ms)
+    # per-step latencies: the same steps again, an event after each
+    lat_steps = min(args.steps, 100)
+    lev = [torch.cuda.Event(enable_timing=True) for _ in range(lat_steps + 1)]
+    with torch.cuda.stream(stream):
+        lev[0].record(stream)
+        for i in range(lat_steps):
+            ctx.plan_set_views(wl.plan, frames[args.warmup + i])
+            ctx.plan_launch(wl.plan)
+            lev[i + 1].record(stream)
+    ctx.synchronize()
+    torch.cuda.synchronize()
+    step_ms = [lev[i].elapsed_time(lev[i + 1]) for i in range(lat_steps)]
     dist.barrier()
     changed = [len(ctx.result_changed(r)) for r in wl.rs]
     ms_step = total_ms / args.steps
@@ -319,7 +332,8 @@ def run_ours(args, dist: Dist) -> dict | None:
                                  "(objects and matrices unchanged); the cold leg has it off"),
                    "tuning": tuning},
         "latency_ms": {"p50": float(np.percentile(step_ms, 50)), "p99": float(np.percentile(step_ms, 99)),
-                       "max": float(max(step_ms))},
+                       "max": float(max(step_ms)), "steps": lat_steps,
+                       "note": "a separate loop over the same steps with an event after each"},
         "plain": {"value": wl.object_views() * dist.world / (plain_ms / 1e3), "ms_per_step": plain_ms,
                   "launches_per_step": wl.v},
         "batched_vs_plain": plain_ms / ms_step,
