@@ -862,13 +862,16 @@ __global__ void __launch_bounds__(kScanThreads, 4)
   __shared__ uint32_t tot;
   __shared__ uint32_t chunk;
   __shared__ bool last;
-  // Launched as a programmatic dependent of the cull: wait for its grid and its memory.
-  asm volatile("griddepcontrol.wait;" ::: "memory");
+  // Launched as a programmatic dependent of the cull.  The view (written before the cull
+  // started) and the chunk ticket (cleared by the previous launch) do not depend on it, so
+  // the block reads and takes them while the cull's last CTAs run; then it waits for the
+  // cull's grid and its memory.
   const CullView& v = views ? views[blockIdx.y] : one;
   if (v.flags & kViewNoChanged) return;  // uniform
   const uint32_t n_words = v.n_words;
   const uint32_t n_chunks = (n_words + kEmitChunk - 1) / kEmitChunk;
   if (blockIdx.x >= n_chunks) {  // uniform; only the view's first n_chunks blocks take tickets
+    asm volatile("griddepcontrol.wait;" ::: "memory");
     if (blockIdx.x == 0 && threadIdx.x == 0) {
       *v.n_changed = 0;
       if (v.copy_count) *v.copy_count = 0;
@@ -881,13 +884,11 @@ __global__ void __launch_bounds__(kScanThreads, 4)
   uint32_t* done = ticket + 1;
   const uint32_t* delta = v.delta;
   if (threadIdx.x == 0) chunk = atomicAdd(ticket, 1u);
-  // Blocks nearly always start in index order, so the ticket gives this block's own chunk:
-  // its words load while the ticket is taken (and again in the rare other case).
-  uint4 q[kEmitRounds];
-  load_rounds(delta, n_words, blockIdx.x * kEmitChunk + (uint32_t)warp * kEmitWarpWords, lane, q);
   __syncthreads();
   const uint32_t c = chunk;
-  if (c != blockIdx.x) load_rounds(delta, n_words, c * kEmitChunk + (uint32_t)warp * kEmitWarpWords, lane, q);
+  asm volatile("griddepcontrol.wait;" ::: "memory");
+  uint4 q[kEmitRounds];
+  load_rounds(delta, n_words, c * kEmitChunk + (uint32_t)warp * kEmitWarpWords, lane, q);
   uint32_t cnt[kEmitRounds];
   uint32_t mine = 0;
 #pragma unroll
