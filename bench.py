@@ -654,7 +654,7 @@ def run_hierarchy_config(ctx, args) -> dict:
             "propagate_roofline": {"bound": "hbm", "achieved": achieved, "peak": pk["hbm_gbs"], "unit": "GB/s",
                                    "frac": achieved / pk["hbm_gbs"], "peak_source": pk["source"],
                                    "algorithmic_bytes": prop_bytes,
-                                   "note": "132 B per transform over one propagation (8 level launches); "
+                                   "note": "132 B per transform over one propagation (one cooperative launch); "
                                            "an 8.6 MB working set is latency-bound, not HBM-bound"},
             "object_views_per_s_e2e": 4_000_000 / (wall_ms / 1e3),
             "note": "per frame: all 64k local matrices updated from page-locked host memory (4 MB), GPU propagation, "

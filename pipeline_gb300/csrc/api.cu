@@ -121,6 +121,11 @@ struct Tree {
   uint32_t* seg = nullptr;
   size_t seg_cap = 0;
   std::vector<TreeLaunch> schedule;
+  // The schedule of the cooperative tree kernel (launch_xform_tree): narrow segments only
+  // up to two entries per thread of block 0, anything wider over the grid.
+  uint4* d_sched = nullptr;
+  size_t sched_cap = 0;
+  uint32_t n_sched = 0, max_wide = 0;
 };
 
 struct Plan {
@@ -1933,6 +1938,7 @@ int dpcull_tree_destroy(dpcull_ctx c, dpcull_tree th)
   dfree(c, t->dirty_world, t->words * 4);
   dfree(c, t->entries, t->entries_cap * 8);
   dfree(c, t->seg, t->seg_cap * 4);
+  dfree(c, t->d_sched, t->sched_cap * sizeof(uint4));
   *t = Tree();
   return DPCULL_OK;
 }
@@ -2047,8 +2053,35 @@ int dpcull_tree_set_structure(dpcull_ctx c, dpcull_tree th, size_t n_entries, co
     if (rc) return rc;
     t->seg_cap = seg.size();
   }
+  // The cooperative kernel's schedule: block 0 takes runs of segments of at most 512
+  // entries (two per thread), every wider segment is one grid step.
+  const uint32_t kNarrowBlock = 512;
+  std::vector<uint4> coop;
+  t->max_wide = 0;
+  for (size_t k = 0; k < nseg;) {
+    if (seg[k + 1] - seg[k] <= kNarrowBlock) {
+      size_t e = k;
+      while (e < nseg && seg[e + 1] - seg[e] <= kNarrowBlock) ++e;
+      coop.push_back(make_uint4(1u, (uint32_t)k, (uint32_t)e, 0u));
+      k = e;
+    } else {
+      coop.push_back(make_uint4(0u, seg[k], seg[k + 1], 0u));
+      t->max_wide = std::max(t->max_wide, seg[k + 1] - seg[k]);
+      ++k;
+    }
+  }
+  if (coop.size() > t->sched_cap) {
+    dfree(c, t->d_sched, t->sched_cap * sizeof(uint4));
+    t->d_sched = nullptr;
+    int rc = dalloc(c, (void**)&t->d_sched, coop.size() * sizeof(uint4));
+    if (rc) return rc;
+    t->sched_cap = coop.size();
+  }
+  t->n_sched = (uint32_t)coop.size();
   if (n_entries) CU(cudaMemcpyAsync(t->entries, pairs, n_entries * 8, cudaMemcpyHostToDevice, c->stream));
   CU(cudaMemcpyAsync(t->seg, seg.data(), seg.size() * 4, cudaMemcpyHostToDevice, c->stream));
+  if (!coop.empty())
+    CU(cudaMemcpyAsync(t->d_sched, coop.data(), coop.size() * sizeof(uint4), cudaMemcpyHostToDevice, c->stream));
   CU(cudaStreamSynchronize(c->stream));
   return DPCULL_OK;
 }
@@ -2093,8 +2126,15 @@ int dpcull_tree_compute(dpcull_ctx c, dpcull_tree th)
 {
   Tree* t = get_tree(c, th);
   if (!t) return fail(DPCULL_ERR_INVALID_ARGUMENT, "bad tree %u", th);
-  CU(cudaMemsetAsync(t->dirty_world, 0, t->words * 4, c->stream));
   XformLaunch a{t->entries, t->seg, t->local, t->world, t->dirty_local, t->dirty_world};
+  // One cooperative launch for the whole tree (it clears both dirty bit arrays itself).
+  if (t->words && launch_xform_tree(a, t->d_sched, t->n_sched, (uint32_t)t->words, t->max_wide, &c->ctl->bar_count,
+                                    &c->ctl->error, c->sm_count, c->stream) == 0) {
+    c->launches++;
+    return tree_groups_stale(c, th);
+  }
+  cudaGetLastError();  // the device refused the cooperative launch: one launch per step
+  CU(cudaMemsetAsync(t->dirty_world, 0, t->words * 4, c->stream));
   for (const TreeLaunch& L : t->schedule) {
     int rc = L.single_cta ? launch_xform_cta(a, L.a, L.b, c->stream)
                           : launch_xform_range(a, L.a, L.b, c->stream);

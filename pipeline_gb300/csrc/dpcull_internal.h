@@ -72,7 +72,8 @@ DPCULL_HD_CONST size_t chunks_of(size_t n_words) { return (n_words + kDeltaChunk
 // Error bits reported through CullControl::error.
 constexpr uint32_t kErrBadTransform = 1u;   // transform index >= matrix count
 constexpr uint32_t kErrMisaligned = 2u;     // a wide launch met a matrix array not 32-byte aligned
-constexpr uint32_t kErrWaitTimeout = 4u;    // a changed-list block gave up waiting for an earlier count
+constexpr uint32_t kErrWaitTimeout = 4u;    // a changed-list block gave up waiting for an earlier
+                                            // count, or a tree block at a grid barrier
 
 // Box cache of a group (the counterpart of the reference's OBB cache, GroupCPU::updateOBBs,
 // dp/culling/cpu/src/ManagerImpl.cpp:114-162): per object the prefilter box of
@@ -172,6 +173,8 @@ struct CullControl {
   unsigned int done;       // CTAs finished
   unsigned int error;      // sticky kErr* bits
   unsigned int error_info; // first offending index
+  unsigned int bar_count;  // the tree kernel's grid barrier: blocks arrived,
+  unsigned int bar_gen;    // and its generation
 };
 
 struct CullLaunch {
@@ -217,13 +220,21 @@ struct XformLaunch {
   const uint32_t* seg;       // segment offsets into entries
   const float* local;        // [cap][16]
   float* world;              // [cap][16]
-  const uint32_t* dirty_local;
+  uint32_t* dirty_local;
   uint32_t* dirty_world;
 };
 // Segments [s0, s1) inside one CTA (narrow levels), or entries [begin, end) of one wide
 // segment over a grid.
 int launch_xform_cta(const XformLaunch& a, uint32_t s0, uint32_t s1, void* stream);
 int launch_xform_range(const XformLaunch& a, uint32_t begin, uint32_t end, void* stream);
+// The whole propagation in one cooperative launch: clears the dirty-world bits, runs the
+// schedule (x = 1: segments [y, z) of narrow levels in block 0, one __syncthreads each;
+// x = 0: entries [y, z) of one wide segment over the grid) with a grid barrier after each
+// step, then clears the dirty-local bits.  `words`: dirty bit words; `max_wide`: entries of
+// the widest segment (sizes the grid).  A block that gives up waiting at a barrier sets
+// kErrWaitTimeout in *err.  Returns -1 if the device cannot run the launch.
+int launch_xform_tree(const XformLaunch& a, const uint4* sched, uint32_t n_sched, uint32_t words,
+                      uint32_t max_wide, unsigned int* bar, unsigned int* err, int sm_count, void* stream);
 int launch_scatter_matrices(float* dst, const float* src, const uint32_t* idx, uint32_t k,
                             uint32_t* dirty_bits, void* stream);
 int launch_scatter_objects(float* soa, uint32_t cap, const float* src, const uint32_t* idx,
