@@ -192,8 +192,9 @@ int dpcull_plan_launch(dpcull_ctx ctx, dpcull_plan p);
 int dpcull_plan_tuning(dpcull_ctx ctx, dpcull_plan p, dpcull_tuning* out);
 /* Duration in ms of the cull kernel alone in one of the plan's two most recent launches
  * (back = 0: the last one, 1: the one before), from CUDA events that the plan's graph
- * records right before and after the kernel; waits until that kernel has finished.  No
- * counterpart in the reference (measurement for the kernel's roofline). */
+ * records on a side branch when the kernel can start and when it has finished; waits until
+ * that kernel has finished.  No counterpart in the reference (measurement for the
+ * kernel's roofline). */
 int dpcull_plan_kernel_ms(dpcull_ctx ctx, dpcull_plan p, uint32_t back, float* ms);
 /* Reads the results of the plan's last launch to the host in two waits: result i is the
  * i-th result of the plan's jobs in job and view order.  bits[i] (ceil(objects/32) words)
@@ -251,9 +252,9 @@ int dpcull_tree_set_locals(dpcull_ctx ctx, dpcull_tree t, size_t k, const uint32
 /* Sets world[index] without marking anything dirty (the fixed root, Tree.cpp:38-47). */
 int dpcull_tree_set_worlds(dpcull_ctx ctx, dpcull_tree t, size_t k, const uint32_t* index,
                            const float* matrices);
-/* (async) Tree::compute (Tree.cpp:133-166): propagates world matrices level by level;
- * afterwards the dirty-world bits of this pass are readable and the dirty-local bits
- * are clear. */
+/* (async) Tree::compute (Tree.cpp:133-166): propagates world matrices level by level
+ * (one cooperative kernel launch); afterwards the dirty-world bits of this pass are
+ * readable and the dirty-local bits are clear. */
 int dpcull_tree_compute(dpcull_ctx ctx, dpcull_tree t);
 /* Device pointer and capacity of the world matrix array (Tree::getWorldMatrices). */
 int dpcull_tree_world_device(dpcull_ctx ctx, dpcull_tree t, const float** world, size_t* count);
