@@ -176,6 +176,8 @@ struct Plan {
   uint32_t n_items = 0;
   uint32_t item_tiles = kItemTiles;
   int grid = 0;
+  uint32_t* d_emit_first = nullptr;    // the changed-list pass's first block of each view
+  uint32_t emit_blocks = 0;            // (emit_blocks_of per view; n_views + 1 entries)
 };
 
 }  // namespace
@@ -640,7 +642,8 @@ int launch_batch(dpcull_ctx c, const CullScene* d_scenes, const CullView* d_view
                  const std::vector<CullScene>& scenes, uint32_t n_views, uint32_t n_items,
                  uint32_t item_tiles, const dpcull_tuning& t, cudaStream_t s,
                  cudaEvent_t k0 = nullptr, cudaEvent_t k1 = nullptr, CacheMode mode = kCacheNone,
-                 cudaStream_t side = nullptr, cudaEvent_t fork = nullptr)
+                 cudaStream_t side = nullptr, cudaEvent_t fork = nullptr, const uint32_t* emit_first = nullptr,
+                 uint32_t emit_blocks = 0)
 {
   if (n_views > 65535) return fail(DPCULL_ERR_INVALID_ARGUMENT, "at most 65535 views per launch");
   const uint32_t max_words = max_words_of(scenes);
@@ -671,7 +674,8 @@ int launch_batch(dpcull_ctx c, const CullScene* d_scenes, const CullView* d_view
     CU(cudaEventRecordWithFlags(k1, side, cudaEventRecordExternal));
   }
   CullView none{};
-  if (!a.emit_views && launch_changed_lists(d_views, none, n_views, max_words, &c->ctl->error, s))
+  if (!a.emit_views && launch_changed_lists(d_views, none, n_views, max_words, &c->ctl->error, s, emit_first,
+                                            emit_blocks))
     return cuda_fail(cudaGetLastError(), "changed-list launch");
   c->launches += a.emit_views ? 1 : 2;
   return DPCULL_OK;
@@ -1356,7 +1360,8 @@ static int plan_capture(dpcull_ctx c, Plan& p, int slot, CacheMode mode)
   if (e == cudaSuccess) {
     const uint64_t before = c->launches;
     rc = launch_batch(c, p.d_scenes, p.d_views, p.scenes, (uint32_t)p.views.size(), p.n_items,
-                      p.item_tiles, p.tuning, cs, p.kt[slot][0], p.kt[slot][1], mode, side, fork);
+                      p.item_tiles, p.tuning, cs, p.kt[slot][0], p.kt[slot][1], mode, side, fork, p.d_emit_first,
+                      p.emit_blocks);
     c->launches = before;  // counted when the graph is replayed
     if (rc == DPCULL_OK) {  // the side stream's timing nodes join the capture again
       e = cudaEventRecord(join, side);
@@ -1523,7 +1528,14 @@ int dpcull_plan_create(dpcull_ctx c, const dpcull_job* jobs, size_t n_jobs,
   CU(cudaMallocHost((void**)&p.h_rcounts, (p.all_results.size() + 2) * sizeof(uint32_t)));
   rc = dalloc(c, (void**)&p.d_scenes, p.scenes.size() * sizeof(CullScene));
   if (!rc) rc = dalloc(c, (void**)&p.d_views, p.views.size() * sizeof(CullView));
+  // The changed-list pass of the plan in one dimension: each view's own chunk count.
+  std::vector<uint32_t> first(p.views.size() + 1, 0u);
+  for (size_t v = 0; v < p.views.size(); ++v) first[v + 1] = first[v] + emit_blocks_of(p.views[v].n_words);
+  p.emit_blocks = first.back();
+  if (!rc) rc = dalloc(c, (void**)&p.d_emit_first, first.size() * sizeof(uint32_t));
   if (rc) return rc;
+  CU(cudaMemcpyAsync(p.d_emit_first, first.data(), first.size() * sizeof(uint32_t), cudaMemcpyHostToDevice,
+                     c->stream));
   CU(cudaMemcpyAsync(p.d_scenes, p.scenes.data(), p.scenes.size() * sizeof(CullScene), cudaMemcpyHostToDevice, c->stream));
   for (int s = 0; s < 2; ++s) {
     CU(cudaMallocHost((void**)&p.h_views[s], p.views.size() * sizeof(CullView)));
@@ -1872,6 +1884,7 @@ int dpcull_plan_destroy(dpcull_ctx c, dpcull_plan ph)
   dfree(c, p->d_copies, std::max<size_t>(2 * p->snap_sizes.size(), 1) * sizeof(ResultCopy));
   dfree(c, p->d_scenes, p->scenes.size() * sizeof(CullScene));
   dfree(c, p->d_views, p->views.size() * sizeof(CullView));
+  dfree(c, p->d_emit_first, (p->views.size() + 1) * sizeof(uint32_t));
   *p = Plan();
   return DPCULL_OK;
 }

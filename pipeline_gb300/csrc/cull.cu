@@ -794,6 +794,7 @@ constexpr int kEmitRounds = 8;                                        // uint4 r
 constexpr uint32_t kEmitWarpWords = 32u * 4u * kEmitRounds;           // 1024
 constexpr uint32_t kEmitChunk = kScanThreads / 32 * kEmitWarpWords;   // 8192 words per block
 static_assert(kEmitChunk % kDeltaChunk == 0, "a view's emit chunks fit its scratch counts");
+static_assert(kEmitChunk == kEmitChunkWords, "the host sizes the pass with kEmitChunkWords");
 constexpr int kWordsPerThread = kDeltaChunk / kScanThreads;
 static_assert(kWordsPerThread % 4 == 0, "whole uint4 loads");
 constexpr uint32_t kSpinLimit = 1u << 20;  // polls of an earlier chunk's count (~0.1 s)
@@ -853,9 +854,10 @@ __device__ __forceinline__ void emit_word(uint32_t m, uint32_t word, uint32_t* c
   }
 }
 
-// grid = (chunks of kEmitChunk words, views)
+// grid = (chunks of kEmitChunk words, views), or (blocks of all views) with first_block
 __global__ void __launch_bounds__(kScanThreads, 4)
-    emit_changed_kernel(const CullView* views, const __grid_constant__ CullView one, unsigned int* err)
+    emit_changed_kernel(const CullView* views, const __grid_constant__ CullView one, unsigned int* err,
+                        const uint32_t* first_block, uint32_t n_views)
 {
   __shared__ uint32_t woff[kScanThreads / 32];
   __shared__ uint32_t wbefore[kScanThreads / 32];
@@ -866,13 +868,24 @@ __global__ void __launch_bounds__(kScanThreads, 4)
   // started) and the chunk ticket (cleared by the previous launch) do not depend on it, so
   // the block reads and takes them while the cull's last CTAs run; then it waits for the
   // cull's grid and its memory.
-  const CullView& v = views ? views[blockIdx.y] : one;
+  uint32_t vi = blockIdx.y, bx = blockIdx.x;
+  if (first_block) {  // the last view whose first block is at or before this one
+    uint32_t lo = 0, hi = n_views;
+    while (hi - lo > 1) {
+      const uint32_t mid = (lo + hi) >> 1;
+      if (__ldg(first_block + mid) <= blockIdx.x) lo = mid;
+      else hi = mid;
+    }
+    vi = lo;
+    bx = blockIdx.x - __ldg(first_block + lo);
+  }
+  const CullView& v = views ? views[vi] : one;
   if (v.flags & kViewNoChanged) return;  // uniform
   const uint32_t n_words = v.n_words;
   const uint32_t n_chunks = (n_words + kEmitChunk - 1) / kEmitChunk;
-  if (blockIdx.x >= n_chunks) {  // uniform; only the view's first n_chunks blocks take tickets
+  if (bx >= n_chunks) {  // uniform; only the view's first n_chunks blocks take tickets
     asm volatile("griddepcontrol.wait;" ::: "memory");
-    if (blockIdx.x == 0 && threadIdx.x == 0) {
+    if (bx == 0 && threadIdx.x == 0) {
       *v.n_changed = 0;
       if (v.copy_count) *v.copy_count = 0;
     }
@@ -1119,13 +1132,14 @@ int cull_max_ctas_per_sm(int vpp, uint32_t mode)
 }
 
 int launch_changed_lists(const CullView* views, const CullView& one, uint32_t n_views,
-                         uint32_t max_words, unsigned int* err, void* stream)
+                         uint32_t max_words, unsigned int* err, void* stream, const uint32_t* first_block,
+                         uint32_t n_blocks)
 {
   cudaStream_t s = static_cast<cudaStream_t>(stream);
   if (!n_views) return 0;
   const uint32_t chunks = std::max<uint32_t>(1, (max_words + kEmitChunk - 1) / kEmitChunk);
   cudaLaunchConfig_t cfg = {};
-  cfg.gridDim = dim3(chunks, n_views);
+  cfg.gridDim = first_block ? dim3(n_blocks) : dim3(chunks, n_views);
   cfg.blockDim = dim3(kScanThreads);
   cfg.stream = s;
   cudaLaunchAttribute attr[1];
@@ -1133,7 +1147,7 @@ int launch_changed_lists(const CullView* views, const CullView& one, uint32_t n_
   attr[0].val.programmaticStreamSerializationAllowed = 1;
   cfg.attrs = attr;
   cfg.numAttrs = 1;
-  if (cudaLaunchKernelEx(&cfg, emit_changed_kernel, views, one, err) != cudaSuccess) return -1;
+  if (cudaLaunchKernelEx(&cfg, emit_changed_kernel, views, one, err, first_block, n_views) != cudaSuccess) return -1;
   return cudaGetLastError() == cudaSuccess ? 0 : -1;
 }
 

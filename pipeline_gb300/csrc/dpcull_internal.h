@@ -205,7 +205,18 @@ int cull_max_ctas_per_sm(int vpp, uint32_t mode);
 // ascending list.  max_words bounds n_words; a block that gives up waiting for an earlier
 // chunk's count sets kErrWaitTimeout in *err.
 int launch_changed_lists(const CullView* views, const CullView& one, uint32_t n_views,
-                         uint32_t max_words, unsigned int* err, void* stream);
+                         uint32_t max_words, unsigned int* err, void* stream,
+                         const uint32_t* first_block = nullptr, uint32_t n_blocks = 0);
+// Delta words per block of the changed-list pass.  With `first_block` (device, n_views + 1
+// entries: view v's blocks are [first_block[v], first_block[v + 1]), at least one each)
+// the pass runs n_blocks blocks in one dimension, so views with fewer chunks than the
+// largest take no idle blocks; without it, max_words' chunks x n_views.
+constexpr uint32_t kEmitChunkWords = 8192;
+inline uint32_t emit_blocks_of(uint32_t n_words)
+{
+  const uint32_t c = (n_words + kEmitChunkWords - 1) / kEmitChunkWords;
+  return c ? c : 1u;
+}
 // Launches of at most this many views whose delta words fit one chunk build their changed
 // lists in the cull kernel's last CTA (CullLaunch::emit_views): no second kernel.
 constexpr uint32_t kFusedEmitViews = 4;
