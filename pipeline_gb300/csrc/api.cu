@@ -514,7 +514,9 @@ int device_errors_read(dpcull_ctx c)
     if (err & kErrMisaligned)
       return fail(DPCULL_ERR_STATE, "work item %u: a matrix array moved off its 32-byte alignment", info);
     if (err & kErrWaitTimeout)
-      return fail(DPCULL_ERR_CUDA, "changed-list assembly: a chunk count never arrived (results incomplete)");
+      return fail(DPCULL_ERR_CUDA,
+                  "a bounded device wait gave up (a changed-list chunk count or a tree grid barrier): "
+                  "results incomplete");
   }
   return DPCULL_OK;
 }
