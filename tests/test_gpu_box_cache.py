@@ -261,3 +261,43 @@ def test_stress_scene_cached_equals_uncached(ctx):
     obbs = oracle.build_obbs(sc["lower"][:, :m], sc["extent"][:, :m], sc["xform"][:m], sc["mats"])
     for v in range(8):
         assert np.array_equal(out[0][5][v][0][: m // 32], oracle.cull_obbs(obbs, frames[5][v], threads=8))
+
+
+@pytest.mark.parametrize("far", [600.0, 1500.0])
+def test_cached_views_whose_far_planes_cut_the_scene(ctx, far):
+    """Cube faces beside a stereo pair at far 5000.  At far 600 the cube faces' far planes
+    pass through the scene (centres within [-1005, 1005]^3), the scene bound does not
+    clear them, and the cached launches keep all six planes; at far 1500 every far plane
+    lies past every centre (about 500 units on), so they run five.  Either way their
+    words and changed lists equal those of the uncached fused kernel (six planes) and the
+    oracle's on a sample."""
+    sc = W.stress_scene(seed=15, n_objects=300_007, n_transforms=20_000)
+    vps = np.stack([np.asarray(v, np.float32).reshape(16)
+                    for v in W.cube_face_views(far=far) + W.stereo_views()])
+    rng = np.random.default_rng(47)
+    frames = [np.stack([W.jitter_view(rng, v) for v in vps]) for _ in range(5)]
+    out = []
+    for cached in (True, False):
+        ctx.set_box_cache(cached)
+        g = ctx.group_create()
+        ctx.group_set_objects(g, sc["lower"], sc["extent"], sc["xform"])
+        ctx.group_set_matrices(g, sc["mats"])
+        rs = [ctx.result_create(g) for _ in range(8)]
+        p = ctx.plan_create([(g, rs, vps)], dict(views_per_pass=8, tiles_per_ticket=1, ctas_per_sm=0))
+        got = []
+        for fr in frames:
+            ctx.plan_set_views(p, fr)
+            ctx.plan_launch(p)
+            got.append([(ctx.result_bits(r).copy(), ctx.result_changed(r).copy()) for r in rs])
+        out.append(got)
+        ctx.plan_destroy(p)
+        ctx.group_destroy(g)
+    ctx.set_box_cache(True)
+    for f in range(5):
+        for v in range(8):
+            assert np.array_equal(out[0][f][v][0], out[1][f][v][0]), (f, v)
+            assert np.array_equal(out[0][f][v][1], out[1][f][v][1]), (f, v)
+    m = 100_000
+    obbs = oracle.build_obbs(sc["lower"][:, :m], sc["extent"][:, :m], sc["xform"][:m], sc["mats"])
+    for v in range(8):
+        assert np.array_equal(out[0][4][v][0][: m // 32], oracle.cull_obbs(obbs, frames[4][v], threads=8))
